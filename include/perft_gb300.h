@@ -1,0 +1,158 @@
+/*
+ * perft_gb300.h -- C ABI of the GB300 (sm_103a) perft engine.
+ *
+ * Drop-in surface for the perft path of sarona-RD/perft_gpu.  Types are
+ * byte-identical to the reference's: pg_board is HexaBitBoardPosition
+ * (chess.h:207-230, 48 bytes) and pg_move is CMove (chess.h:234-268, 16 bits:
+ * from 0-5, to 6-11, flags 12-15).  Every entry point returns a pg_status
+ * (0 = PG_OK) instead of printing and exiting; pg_last_error() gives the
+ * message of the last failure on the calling thread.  Host arrays are owned
+ * by the caller; device memory is owned by the engine.  There is no CPU
+ * fallback: every count below is computed by CUDA kernels on the GPU, and
+ * the calls fail with PG_ERR_CUDA when no usable GPU is present.
+ *
+ * Thread safety: the engine serialises calls internally; one engine per
+ * process (the reference's MoveGeneratorBitboard::init is also per process,
+ * MoveGeneratorBitboard.h:982).
+ */
+#ifndef PERFT_GB300_H
+#define PERFT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* HexaBitBoardPosition (chess.h:207-230): six bitboards; the game state is
+ * packed into the pawns word: bits 0-1 white castling (1 = king side,
+ * 2 = queen side), bits 2-3 black castling, bits 4-7 en-passant file + 1,
+ * bits 56-62 half-move counter, bit 63 side to move (0 white, 1 black). */
+typedef struct pg_board {
+    uint64_t white;
+    uint64_t pawns;
+    uint64_t knights;
+    uint64_t bishop_queens;
+    uint64_t rook_queens;
+    uint64_t kings;
+} pg_board;
+
+/* CMove (chess.h:234-268). */
+typedef uint16_t pg_move;
+
+typedef enum pg_status {
+    PG_OK = 0,
+    PG_ERR_NOT_INITIALIZED = 1,
+    PG_ERR_INVALID_ARGUMENT = 2,
+    PG_ERR_INVALID_POSITION = 3, /* not exactly one king per side, overlapping bitboards */
+    PG_ERR_CUDA = 4,
+    PG_ERR_OUT_OF_MEMORY = 5,    /* HBM budget too small for the request */
+    PG_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up */
+    PG_ERR_BUSY = 7,
+    PG_ERR_CAPACITY = 8          /* fixed-size buffer of a call exceeded */
+} pg_status;
+
+typedef enum pg_slider {
+    PG_SLIDER_AUTO = 0,      /* autotuner's choice */
+    PG_SLIDER_KOGGE_STONE = 1,
+    PG_SLIDER_FANCY = 2,     /* fancy magics, attack table in global memory (L2) */
+    PG_SLIDER_BYTE_SMEM = 3  /* byte-lookup fancy magics staged in shared memory */
+} pg_slider;
+
+typedef struct pg_config {
+    int device;                  /* CUDA device ordinal (default 0) */
+    uint64_t hbm_budget_bytes;   /* level buffers + TT; 0 = 60% of free HBM */
+    int slider;                  /* default slider policy (pg_slider) */
+    int verbose;
+} pg_config;
+
+typedef struct pg_stats {
+    double device_ms;            /* CUDA-event time of the engine's launches */
+    uint64_t leaves;             /* sum of the results */
+    uint64_t launches;           /* kernels launched by the call */
+    uint64_t peak_level_bytes;   /* largest frontier level held */
+    uint64_t tt_probes, tt_hits, tt_stores;
+    uint64_t leaf_kernel_launches;
+    double leaf_kernel_ms;       /* CUDA-event time of the leaf (2-ply) kernel launches */
+    uint64_t leaf_parent_nodes;  /* nodes handed to the leaf kernel (each 2 plies above a leaf) */
+} pg_stats;
+
+typedef struct pg_opts {
+    int slider;                  /* pg_slider; PG_SLIDER_AUTO = tuned per call */
+    int block_size;              /* leaf/expand CTA size: 0 = tuned, else 128/256/512 */
+    int leaf_plies;              /* plies handled inside one CTA at the leaf: 0 = tuned, 1 or 2 */
+    int use_tt;                  /* transposition tables on (1) / off (0) */
+    uint64_t tt_bytes;           /* total TT bytes across depths; 0 = from budget */
+    int graph;                   /* replay the call's launch sequence from a captured CUDA graph */
+    pg_stats *stats;             /* optional out */
+} pg_opts;
+
+/* ---- engine ---- */
+/* MoveGeneratorBitboard::init (MoveGeneratorBitboard.h:982-1203) plus the
+ * allocation of initGPU (launcher.h:1506-1533). cfg may be NULL. */
+int pg_init(const pg_config *cfg);
+int pg_shutdown(void);
+const char *pg_last_error(void);
+/* Utils::readFENString + board088ToHexBB (util.cpp:189-280, util.cpp:92-140). */
+int pg_board_from_fen(const char *fen, pg_board *out);
+
+/* ---- operator surface (GPU kernels, one position per call or a batch) ---- */
+/* countMoves<c> (MoveGeneratorBitboard.h:3008-3295). */
+int pg_count_moves(const pg_board *pos, uint32_t *out);
+int pg_count_moves_batch(const pg_board *pos, uint32_t n, uint32_t *out);
+/* generateMoves<c> (MoveGeneratorBitboard.h:2469-2823), host flavour:
+ * same order and flags as the reference's host build; moves holds 256. */
+int pg_generate_moves(const pg_board *pos, pg_move *moves, uint32_t *n);
+/* generateBoards<c> (MoveGeneratorBitboard.h:1940-2261); out holds 256. */
+int pg_generate_boards(const pg_board *pos, pg_board *out, uint32_t *n);
+/* makeMove<c,false> (MoveGeneratorBitboard.h:3310-3570), in place. */
+int pg_make_move(pg_board *pos, pg_move move);
+
+/* ---- perft ---- */
+/* perft_bb (perft_bb.h:79-101) / perftLauncher (launcher.h:1455-1504),
+ * which prints instead of returning; depth 0..15. */
+int pg_perft(const pg_board *pos, int depth, uint64_t *out, const pg_opts *opts);
+/* divided perft: counts[i] = perft(child after moves[i], depth-1) for every
+ * legal root move in generateMoves order (perft_bb_cpu_launcher's per-move
+ * lines, launcher.h:1344-1351); moves/counts hold 256. */
+int pg_perft_divide(const pg_board *pos, int depth, pg_move *moves, uint64_t *counts,
+                    uint32_t *n, const pg_opts *opts);
+/* n positions, each with its own depth, in one load-balanced engine run.
+ * Host arrays. */
+int pg_perft_batch(const pg_board *pos, const uint8_t *depths, uint32_t n, uint64_t *out,
+                   const pg_opts *opts);
+/* The same with device pointers (inputs already resident in HBM). */
+int pg_perft_batch_device(const pg_board *d_pos, const uint8_t *d_depths, uint32_t n,
+                          uint64_t *d_out, const pg_opts *opts);
+
+/* ---- inputs ---- */
+/* Seeded random legal playouts from the initial position, generated on the
+ * GPU.  Position i is the first accepted attempt a = 0, 1, ... of:
+ * s = seed ^ (i << 32) ^ (a * 0xA24BAED4963EE407); plies = min_plies +
+ * next(s) % (max_plies - min_plies + 1); per ply pick
+ * generateMoves[next(s) % count] and makeMove; accepted when every ply had a
+ * move and the final position has at least min_moves legal moves.  next() is
+ * splitmix64.  depths (may be NULL): depth_lo + next(s') % (depth_hi -
+ * depth_lo + 1) with s' = seed ^ (i << 32) ^ 0x5851F42D4C957F2D. */
+int pg_random_playouts(uint64_t seed, uint32_t n, int min_plies, int max_plies, int min_moves,
+                       int depth_lo, int depth_hi, pg_board *out, uint8_t *depths);
+
+/* ---- serving: continuous batching of perft requests ---- */
+typedef struct pg_server_config {
+    uint64_t hbm_budget_bytes;   /* admission budget for in-flight frontiers; 0 = engine budget */
+    uint32_t max_inflight;       /* request slots; 0 = 4096 */
+    int slider;
+    uint32_t max_wave_nodes;     /* frontier nodes the scheduler advances per wave; 0 = auto */
+} pg_server_config;
+
+int pg_server_start(const pg_server_config *cfg);
+/* Returns at once with a request id; the request joins the running waves. */
+int pg_server_submit(const pg_board *pos, int depth, uint64_t *request_id);
+/* done = 1 once the count is final; latency_ms from submit to completion. */
+int pg_server_poll(uint64_t request_id, uint64_t *result, int *done, double *latency_ms);
+int pg_server_stop(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

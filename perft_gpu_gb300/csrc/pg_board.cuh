@@ -1,0 +1,169 @@
+// pg_board.cuh -- board type, constants and bit primitives for the sm_103a
+// move generator.
+//
+// The 48-byte board is the reference's HexaBitBoardPosition
+// (chess.h:207-230): six 64-bit words, with the game state packed into the
+// rank-1 and rank-8 bytes of the pawn word (castling bits 0-3, en-passant
+// file+1 bits 4-7, half-move counter bits 56-62, side to move bit 63).
+#pragma once
+#include <cstdint>
+
+#include "pg_types.h"
+
+namespace pg {
+
+struct Pos {
+    u64 w;   // whitePieces
+    u64 p;   // pawns (ranks 2-7) + packed state
+    u64 n;   // knights
+    u64 bq;  // bishops and queens
+    u64 rq;  // rooks and queens
+    u64 k;   // kings
+};
+
+constexpr u64 FILE_A = 0x0101010101010101ull;
+constexpr u64 FILE_H = 0x8080808080808080ull;
+constexpr u64 NOT_A = ~FILE_A;
+constexpr u64 NOT_H = ~FILE_H;
+constexpr u64 RANK_1 = 0x00000000000000FFull;
+constexpr u64 RANK_3 = 0x0000000000FF0000ull;
+constexpr u64 RANK_6 = 0x0000FF0000000000ull;
+constexpr u64 RANK_8 = 0xFF00000000000000ull;
+constexpr u64 BACK_RANKS = RANK_1 | RANK_8;
+constexpr u64 INNER = 0x00FFFFFFFFFFFF00ull;
+constexpr u64 DIAG_A1H8 = 0x8040201008040201ull;
+constexpr u64 DIAG_A8H1 = 0x0102040810204080ull;
+
+// castling square sets of the reference (MoveGeneratorBitboard.h:43-55)
+constexpr u64 W_KS_PATH = 0x60ull;
+constexpr u64 W_QS_SAFE = 0x0Cull;
+constexpr u64 W_QS_PATH = 0x0Eull;
+constexpr u64 B_KS_PATH = 0x6000000000000000ull;
+constexpr u64 B_QS_SAFE = 0x0C00000000000000ull;
+constexpr u64 B_QS_PATH = 0x0E00000000000000ull;
+
+// CMove flags (chess.h:272-293)
+enum : int {
+    MF_QUIET = 0, MF_DOUBLE = 1, MF_KCASTLE = 2, MF_QCASTLE = 3, MF_CAPTURE = 4, MF_EP = 5,
+    MF_PROMO_N = 8, MF_PROMO_B = 9, MF_PROMO_R = 10, MF_PROMO_Q = 11
+};
+
+__host__ __device__ __forceinline__ u16 cmove(int from, int to, int fl)
+{
+    return (u16)(((fl & 0xF) << 12) | ((to & 0x3F) << 6) | (from & 0x3F));
+}
+
+__device__ __forceinline__ int lsb(u64 x) { return __ffsll((long long)x) - 1; }
+__device__ __forceinline__ int popc(u64 x) { return __popcll(x); }
+__device__ __forceinline__ u64 lowbit(u64 x) { return x & (0ull - x); }
+__device__ __forceinline__ bool several(u64 x) { return (x & (x - 1)) != 0; }
+
+// ---- packed state ----
+__device__ __forceinline__ int st_side(const Pos& b) { return (int)(b.p >> 63); }
+__device__ __forceinline__ int st_wc(const Pos& b) { return (int)(b.p & 3); }
+__device__ __forceinline__ int st_bc(const Pos& b) { return (int)((b.p >> 2) & 3); }
+__device__ __forceinline__ int st_ep(const Pos& b) { return (int)((b.p >> 4) & 15); }
+__device__ __forceinline__ void set_wc(Pos& b, int v) { b.p = (b.p & ~3ull) | (u64)(v & 3); }
+__device__ __forceinline__ void set_bc(Pos& b, int v) { b.p = (b.p & ~12ull) | ((u64)(v & 3) << 2); }
+__device__ __forceinline__ void set_ep(Pos& b, int v) { b.p = (b.p & ~0xF0ull) | ((u64)(v & 15) << 4); }
+__device__ __forceinline__ void set_side(Pos& b, int v) { b.p = (b.p & ~(1ull << 63)) | ((u64)(v & 1) << 63); }
+__device__ __forceinline__ void set_hm(Pos& b, int v) { b.p = (b.p & ~(0x7Full << 56)) | ((u64)(v & 0x7F) << 56); }
+
+// ---- one-square steps ----
+__device__ __forceinline__ u64 up(u64 x) { return x << 8; }
+__device__ __forceinline__ u64 down(u64 x) { return x >> 8; }
+__device__ __forceinline__ u64 east1(u64 x) { return (x << 1) & NOT_A; }
+__device__ __forceinline__ u64 west1(u64 x) { return (x >> 1) & NOT_H; }
+__device__ __forceinline__ u64 up_e(u64 x) { return (x << 9) & NOT_A; }
+__device__ __forceinline__ u64 up_w(u64 x) { return (x << 7) & NOT_H; }
+__device__ __forceinline__ u64 dn_e(u64 x) { return (x >> 7) & NOT_A; }
+__device__ __forceinline__ u64 dn_w(u64 x) { return (x >> 9) & NOT_H; }
+
+template <int S> __device__ __forceinline__ u64 push1(u64 x) { return S ? down(x) : up(x); }
+template <int S> __device__ __forceinline__ u64 cap_w(u64 x) { return S ? dn_w(x) : up_w(x); }
+template <int S> __device__ __forceinline__ u64 cap_e(u64 x) { return S ? dn_e(x) : up_e(x); }
+// squares from which an enemy pawn (of side !S) attacks x, seen from side S
+template <int S> __device__ __forceinline__ u64 pawn_attackers_of(u64 x) { return S ? (dn_e(x) | dn_w(x)) : (up_e(x) | up_w(x)); }
+// squares attacked by pawns of side T
+template <int T> __device__ __forceinline__ u64 pawn_attacks(u64 p) { return T ? (dn_e(p) | dn_w(p)) : (up_e(p) | up_w(p)); }
+template <int S> __device__ __forceinline__ constexpr u64 double_rank() { return S ? RANK_6 : RANK_3; }
+
+__device__ __forceinline__ u64 knight_set(u64 n)
+{
+    u64 a = ((n >> 1) & NOT_H) | ((n << 1) & NOT_A);
+    u64 b = ((n >> 2) & 0x3F3F3F3F3F3F3F3Full) | ((n << 2) & 0xFCFCFCFCFCFCFCFCull);
+    return (a << 16) | (a >> 16) | (b << 8) | (b >> 8);
+}
+__device__ __forceinline__ u64 king_set(u64 k)
+{
+    u64 a = east1(k) | west1(k);
+    u64 row = k | a;
+    return a | up(row) | down(row);
+}
+
+// ---- Kogge-Stone occluded fill in one direction ----
+// SH: step (1, 7, 8 or 9); LEFT: toward higher squares; KEEP: wrap mask.
+// Returns the squares attacked in that direction, first blocker included.
+template <int SH, bool LEFT> __device__ __forceinline__ u64 shf(u64 x) { return LEFT ? (x << SH) : (x >> SH); }
+
+template <int SH, bool LEFT> struct DirMask {
+    static constexpr u64 keep = (SH == 8) ? ~0ull
+                              : (SH == 1) ? (LEFT ? NOT_A : NOT_H)
+                              : (SH == 9) ? (LEFT ? NOT_A : NOT_H)
+                                          : (LEFT ? NOT_H : NOT_A);  // SH == 7
+};
+
+// propagator chain of one direction, shared by every generator filled along it
+template <int SH, bool LEFT> struct Pro {
+    u64 p1, p2, p4;
+    __device__ __forceinline__ explicit Pro(u64 empty)
+    {
+        p1 = empty & DirMask<SH, LEFT>::keep;
+        p2 = p1 & shf<SH, LEFT>(p1);
+        p4 = p2 & shf<2 * SH, LEFT>(p2);
+    }
+    __device__ __forceinline__ u64 attacks(u64 g) const
+    {
+        g |= p1 & shf<SH, LEFT>(g);
+        g |= p2 & shf<2 * SH, LEFT>(g);
+        g |= p4 & shf<4 * SH, LEFT>(g);
+        return shf<SH, LEFT>(g) & DirMask<SH, LEFT>::keep;
+    }
+};
+
+template <int SH, bool LEFT> __device__ __forceinline__ u64 ray(u64 g, u64 empty)
+{
+    return Pro<SH, LEFT>(empty).attacks(g);
+}
+
+__device__ __forceinline__ u64 ks_bishop(u64 g, u64 empty)
+{
+    return ray<9, true>(g, empty) | ray<7, true>(g, empty) | ray<7, false>(g, empty) | ray<9, false>(g, empty);
+}
+__device__ __forceinline__ u64 ks_rook(u64 g, u64 empty)
+{
+    return ray<8, true>(g, empty) | ray<8, false>(g, empty) | ray<1, true>(g, empty) | ray<1, false>(g, empty);
+}
+
+// the four lines through a square (used to split pinned pieces by pin line)
+__device__ __forceinline__ u64 file_of(int sq) { return FILE_A << (sq & 7); }
+__device__ __forceinline__ u64 rank_of(int sq) { return RANK_1 << (sq & 56); }
+__device__ __forceinline__ u64 diag_of(int sq)
+{
+    int d = (sq >> 3) - (sq & 7);
+    return d >= 0 ? (DIAG_A1H8 << (8 * d)) : (DIAG_A1H8 >> (-8 * d));
+}
+__device__ __forceinline__ u64 anti_of(int sq)
+{
+    int d = (sq >> 3) + (sq & 7) - 7;
+    return d >= 0 ? (DIAG_A8H1 << (8 * d)) : (DIAG_A8H1 >> (-8 * d));
+}
+
+// squares strictly between lo and hi on the line `line`
+__device__ __forceinline__ u64 between_on(u64 line, int a, int b)
+{
+    int lo = min(a, b), hi = max(a, b);
+    return line & ((1ull << hi) - (2ull << lo));
+}
+
+}  // namespace pg

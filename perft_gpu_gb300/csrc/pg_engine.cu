@@ -1,0 +1,642 @@
+// pg_engine.cu -- launch plans, the chunked breadth-first
+// driver and the C ABI of the GB300 perft engine.
+//
+// Host-side control follows the reference's no-TT launcher
+// (perftLauncher, launcher.h:1467-1503; perft_bb_gpu_simple,
+// perft_bb.h:1027-1138) but without dynamic parallelism: the host walks the
+// levels, a level that would not fit its buffer is split into chunks that do
+// (the reference instead picks a launch depth from a branching-factor
+// estimate, launcher.h:1535-1563), and every wait on the device is bounded.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pg_engine.cuh"
+#include "pg_level.cuh"
+#include "pg_ops.cuh"
+#include "pg_tt.cuh"
+
+namespace pg {
+
+static Engine g_engine;
+Engine& engine() { return g_engine; }
+
+static thread_local std::string t_error;
+
+void set_error(const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_error = buf;
+}
+
+#define PG_CUDA(call)                                                                        \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return e_ == cudaErrorMemoryAllocation ? PG_ERR_OUT_OF_MEMORY : PG_ERR_CUDA;    \
+        }                                                                                    \
+    } while (0)
+
+#define PG_TRY(expr)              \
+    do {                          \
+        int r_ = (expr);          \
+        if (r_ != PG_OK) return r_; \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// launch plans
+// ---------------------------------------------------------------------------
+
+struct Variant {
+    int slider;  // pg_slider (never AUTO here)
+    int T;       // CTA size of the block-queue kernels
+};
+
+static u32* next_ticket()
+{
+    Engine& E = engine();
+    if (E.ticket_next >= MAX_TICKETS - 8) return nullptr;
+    return E.tickets + E.ticket_next++;
+}
+
+#define PG_TICKET(var)                              \
+    u32* var = next_ticket();                       \
+    if (!var) {                                     \
+        set_error("dynamic-scheduling counters exhausted"); \
+        return PG_ERR_CAPACITY;                     \
+    }
+
+static int launch_leaf(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u64* acc)
+{
+    Engine& E = engine();
+    PG_TICKET(tk);
+    PG_CUDA(ops_for(v.slider).leaf(side, v.T, lv, start, n, acc, tk, E.stream, E.num_sms));
+    E.st.launches++;
+    E.st.leaf_kernel_launches++;
+    E.st.leaf_parent_nodes += n;
+    return PG_OK;
+}
+
+static int launch_expand(const Variant& v, int side, const LevelView& in, u32 start, u32 a, u32 b, const u64* offs,
+                         const LevelView& out)
+{
+    Engine& E = engine();
+    PG_TICKET(tk);
+    PG_CUDA(ops_for(v.slider).expand(side, v.T, in, start, a, b, offs, out, tk, E.stream, E.num_sms));
+    E.st.launches++;
+    return PG_OK;
+}
+
+static int launch_count(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u32* cnt)
+{
+    Engine& E = engine();
+    PG_CUDA(ops_for(v.slider).count_level(side, lv, start, n, cnt, E.stream, E.num_sms));
+    E.st.launches++;
+    return PG_OK;
+}
+
+static int launch_scan(const u32* cnt, u32 n, u64* offs)
+{
+    Engine& E = engine();
+    const u64 tiles = (n + SCAN_TILE - 1) / SCAN_TILE + 1;
+    if (tiles > E.scan_status_cap) {
+        if (E.scan_status) cudaFree(E.scan_status);
+        E.scan_status = nullptr;
+        E.scan_status_cap = 0;
+        PG_CUDA(cudaMalloc(&E.scan_status, tiles * sizeof(u64)));
+        E.scan_status_cap = tiles;
+    }
+    u32* tk = next_ticket();
+    if (!tk) {
+        set_error("ticket pool exhausted");
+        return PG_ERR_CAPACITY;
+    }
+    PG_CUDA(cudaMemsetAsync(E.scan_status, 0, tiles * sizeof(u64), E.stream));
+    const u32 grid = (u32)std::max<u64>(1, (n + SCAN_TILE - 1) / SCAN_TILE);
+    k_scan<<<grid, SCAN_T, 0, E.stream>>>(cnt, n, offs, E.scan_status, tk, E.err);
+    PG_CUDA(cudaGetLastError());
+    E.st.launches++;
+    return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// level buffers
+// ---------------------------------------------------------------------------
+
+static constexpr u64 NODE_BYTES = 48 + 4 + 1 + 4 + 8;
+
+static u64 level_cap_max()
+{
+    Engine& E = engine();
+    u64 cap = E.budget / NODE_BYTES / 4;
+    cap = std::min<u64>(cap, 0xF0000000ull);
+    return std::max<u64>(cap, 1u << 16);
+}
+
+static int ensure_level(int L, u64 need)
+{
+    Engine& E = engine();
+    if (L >= MAX_LEVELS) {
+        set_error("depth exceeds %d levels", MAX_LEVELS);
+        return PG_ERR_CAPACITY;
+    }
+    LevelBuf& lb = E.lv[L];
+    if (lb.cap >= need) return PG_OK;
+    u64 cap = 1u << 16;
+    while (cap < need) cap <<= 1;
+    cap = std::min(cap, std::max(level_cap_max(), need));
+    if (lb.block) {
+        PG_CUDA(cudaStreamSynchronize(E.stream));
+        cudaFree(lb.block);
+        E.level_bytes_total -= lb.cap * NODE_BYTES;
+        lb = LevelBuf{};
+    }
+    const u64 bytes = cap * 48 + cap * 4 + cap + 16 + cap * 4 + (cap + 1) * 8 + 256;
+    void* blk = nullptr;
+    cudaError_t e = cudaMalloc(&blk, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("level %d buffer of %llu nodes (%llu bytes) failed: %s", L, (unsigned long long)cap,
+                  (unsigned long long)bytes, cudaGetErrorString(e));
+        return PG_ERR_OUT_OF_MEMORY;
+    }
+    unsigned char* p = (unsigned char*)blk;
+    lb.v.pl0 = (ulonglong2*)p;
+    p += cap * 16;
+    lb.v.pl1 = (ulonglong2*)p;
+    p += cap * 16;
+    lb.v.pl2 = (ulonglong2*)p;
+    p += cap * 16;
+    lb.offs = (u64*)p;
+    p += (cap + 1) * 8;
+    p = (unsigned char*)(((uintptr_t)p + 15) & ~(uintptr_t)15);
+    lb.v.grp = (u32*)p;
+    p += cap * 4;
+    lb.cnt = (u32*)p;
+    p += cap * 4;
+    lb.v.rem = p;
+    lb.cap = cap;
+    lb.block = blk;
+    E.level_bytes_total += cap * NODE_BYTES;
+    return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// breadth-first driver
+// ---------------------------------------------------------------------------
+
+static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int minrem, int maxrem, u64* acc)
+{
+    Engine& E = engine();
+    if (n == 0) return PG_OK;
+    LevelBuf& lb = E.lv[L];
+    E.st.peak_level_bytes = std::max<uint64_t>(E.st.peak_level_bytes, (uint64_t)n * 48);
+    if (minrem <= 2) {
+        cudaEventRecord(E.lev0, E.stream);
+        PG_TRY(launch_leaf(v, side, lb.v, start, n, acc));
+        cudaEventRecord(E.lev1, E.stream);
+        // the leaf kernel's time is read back at the next sync
+        float ms = 0;
+        PG_CUDA(cudaEventSynchronize(E.lev1));
+        cudaEventElapsedTime(&ms, E.lev0, E.lev1);
+        E.st.leaf_kernel_ms += ms;
+    }
+    if (maxrem < 3) return PG_OK;
+    PG_TRY(launch_count(v, side, lb.v, start, n, lb.cnt));
+    PG_TRY(launch_scan(lb.cnt, n, lb.offs));
+    const u64 cap_next = level_cap_max();
+    k_plan<<<1, 32, 0, E.stream>>>(lb.offs, n, cap_next, E.plan_dev, E.err);
+    PG_CUDA(cudaGetLastError());
+    E.st.launches++;
+    PG_CUDA(cudaMemcpyAsync(E.plan_host, E.plan_dev, sizeof(PlanOut), cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    u32 errv = 0;
+    PG_CUDA(cudaMemcpy(&errv, E.err, sizeof(u32), cudaMemcpyDeviceToHost));
+    if (errv) {
+        set_error("device error flags 0x%x while planning level %d", errv, L);
+        return PG_ERR_DEVICE_TIMEOUT;
+    }
+    const PlanOut plan = *E.plan_host;  // copy: deeper levels reuse the pinned buffer
+    std::vector<u32> bnd(plan.bnd, plan.bnd + plan.nchunks + 1);
+    if (plan.total == 0) return PG_OK;
+    std::vector<u64> boff(plan.coff, plan.coff + plan.nchunks + 1);
+    const int cminrem = std::max(minrem, 3) - 1, cmaxrem = maxrem - 1;
+    for (size_t k = 0; k + 1 < bnd.size(); k++) {
+        const u32 a = bnd[k], b = bnd[k + 1];
+        const u64 children = boff[k + 1] - boff[k];
+        if (!children) continue;
+        PG_TRY(ensure_level(L + 1, children));
+        PG_TRY(launch_expand(v, side, lb.v, start, a, b, lb.offs, E.lv[L + 1].v));
+        PG_TRY(run_range(v, L + 1, 0, (u32)children, 1 - side, cminrem, cmaxrem, acc));
+    }
+    return PG_OK;
+}
+
+static Variant pick_variant(const pg_opts* o)
+{
+    Engine& E = engine();
+    Variant v{PG_SLIDER_KOGGE_STONE, 256};
+    int sl = o ? o->slider : PG_SLIDER_AUTO;
+    if (sl == PG_SLIDER_AUTO) sl = E.default_slider;
+    if (sl == PG_SLIDER_AUTO) sl = PG_SLIDER_KOGGE_STONE;
+    v.slider = sl;
+    if (o && (o->block_size == 128 || o->block_size == 256 || o->block_size == 512)) v.T = o->block_size;
+    return v;
+}
+
+static bool valid_board(const pg_board& b)
+{
+    const u64 inner = INNER;
+    const u64 pawns = b.pawns & inner;
+    const u64 occ = pawns | b.knights | b.bishop_queens | b.rook_queens | b.kings;
+    if (pawns & (b.knights | b.bishop_queens | b.rook_queens | b.kings)) return false;
+    if (b.knights & (b.bishop_queens | b.rook_queens | b.kings)) return false;
+    if ((b.bishop_queens | b.rook_queens) & b.kings) return false;
+    if (b.white & ~occ) return false;
+    if (__builtin_popcountll(b.kings & b.white) != 1) return false;
+    if (__builtin_popcountll(b.kings & ~b.white) != 1) return false;
+    return true;
+}
+
+static int check_ready()
+{
+    if (!engine().ready) {
+        set_error("pg_init has not been called");
+        return PG_ERR_NOT_INITIALIZED;
+    }
+    return PG_OK;
+}
+
+static int ensure_stage(u64 bytes)
+{
+    Engine& E = engine();
+    if (E.stage_cap >= bytes) return PG_OK;
+    if (E.stage) cudaFree(E.stage);
+    E.stage = nullptr;
+    E.stage_cap = 0;
+    u64 cap = 1 << 20;
+    while (cap < bytes) cap <<= 1;
+    PG_CUDA(cudaMalloc(&E.stage, cap));
+    E.stage_cap = cap;
+    return PG_OK;
+}
+
+static int begin_call(const pg_opts* o)
+{
+    Engine& E = engine();
+    E.st = pg_stats{};
+    E.ticket_next = 0;
+    PG_CUDA(cudaMemsetAsync(E.tickets, 0, MAX_TICKETS * sizeof(u32), E.stream));
+    PG_CUDA(cudaMemsetAsync(E.err, 0, sizeof(u32), E.stream));
+    (void)o;
+    return PG_OK;
+}
+
+static int end_call(const pg_opts* o)
+{
+    Engine& E = engine();
+    u32 errv = 0;
+    PG_CUDA(cudaMemcpyAsync(E.host_scratch, E.err, sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    errv = (u32)E.host_scratch[0];
+    if (errv & 0xFFFFFFFFu) {
+        set_error("device error flags 0x%x", errv);
+        return PG_ERR_DEVICE_TIMEOUT;
+    }
+    if (o && o->stats) *o->stats = E.st;
+    return PG_OK;
+}
+
+// batch perft with device inputs; d_out must not alias the inputs
+static int perft_batch_device_locked(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out,
+                                     const pg_opts* o)
+{
+    Engine& E = engine();
+    const Variant v = pick_variant(o);
+    PG_TRY(ensure_level(0, n));
+    PG_CUDA(cudaMemsetAsync(d_out, 0, (u64)n * sizeof(u64), E.stream));
+    u32* ctr = (u32*)(E.host_scratch + 64);  // pinned, 4 words
+    u32* dctr = E.tickets + MAX_TICKETS - 4;
+    const u32 init[4] = {0, 0, 0xFFFFFFFFu, 0};
+    PG_CUDA(cudaMemcpyAsync(dctr, init, sizeof(init), cudaMemcpyHostToDevice, E.stream));
+    k_partition_roots<<<std::max<u32>(1, std::min<u32>((n + 255) / 256, 4096)), 256, 0, E.stream>>>(d_pos, d_depths, n,
+                                                                                                 E.lv[0].v, dctr);
+    PG_CUDA(cudaGetLastError());
+    E.st.launches++;
+    PG_CUDA(cudaMemcpyAsync(ctr, dctr, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    const u32 nw = ctr[0], mind = ctr[2], maxd = ctr[3];
+    if (maxd > 15) {
+        set_error("depth %u out of range 0..15", maxd);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    cudaEventRecord(E.ev0, E.stream);
+    PG_TRY(run_range(v, 0, 0, nw, 0, (int)mind, (int)maxd, d_out));
+    PG_TRY(run_range(v, 0, nw, n - nw, 1, (int)mind, (int)maxd, d_out));
+    cudaEventRecord(E.ev1, E.stream);
+    PG_CUDA(cudaEventSynchronize(E.ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+    E.st.device_ms = ms;
+    return PG_OK;
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+const char* pg_last_error(void) { return t_error.c_str(); }
+
+int pg_init(const pg_config* cfg)
+{
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    if (E.ready) return PG_OK;
+    E.device = cfg ? cfg->device : 0;
+    E.verbose = cfg ? cfg->verbose : 0;
+    E.default_slider = cfg ? cfg->slider : PG_SLIDER_AUTO;
+    int ndev = 0;
+    PG_CUDA(cudaGetDeviceCount(&ndev));
+    if (E.device < 0 || E.device >= ndev) {
+        set_error("device %d not present (%d devices)", E.device, ndev);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    PG_CUDA(cudaSetDevice(E.device));
+    cudaDeviceProp prop;
+    PG_CUDA(cudaGetDeviceProperties(&prop, E.device));
+    if (prop.major < 10) {
+        set_error("device %d is sm_%d%d; this build targets sm_103a", E.device, prop.major, prop.minor);
+        return PG_ERR_CUDA;
+    }
+    E.num_sms = prop.multiProcessorCount;
+    size_t freeb = 0, totalb = 0;
+    PG_CUDA(cudaMemGetInfo(&freeb, &totalb));
+    E.budget = (cfg && cfg->hbm_budget_bytes) ? cfg->hbm_budget_bytes : (u64)(freeb * 0.6);
+    PG_CUDA(cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking));
+    PG_CUDA(cudaEventCreate(&E.ev0));
+    PG_CUDA(cudaEventCreate(&E.ev1));
+    PG_CUDA(cudaEventCreate(&E.lev0));
+    PG_CUDA(cudaEventCreate(&E.lev1));
+    const HostTables* tabs = host_tables();
+    if (!tabs) {
+        set_error("magic table construction failed");
+        return PG_ERR_CUDA;
+    }
+    PG_CUDA(g_ops_ks.upload(*tabs));
+    PG_CUDA(g_ops_fancy.upload(*tabs));
+    PG_CUDA(g_ops_byte.upload(*tabs));
+    PG_CUDA(cudaMalloc(&E.tickets, MAX_TICKETS * sizeof(u32)));
+    PG_CUDA(cudaMalloc(&E.err, 16));
+    PG_CUDA(cudaMalloc(&E.plan_dev, sizeof(PlanOut)));
+    PG_CUDA(cudaMallocHost(&E.plan_host, sizeof(PlanOut)));
+    PG_CUDA(cudaMallocHost(&E.host_scratch, 4096));
+    PG_CUDA(cudaDeviceSynchronize());
+    E.ready = true;
+    return PG_OK;
+}
+
+int pg_shutdown(void)
+{
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    if (!E.ready) return PG_OK;
+    cudaStreamSynchronize(E.stream);
+    for (auto& lb : E.lv) {
+        if (lb.block) cudaFree(lb.block);
+        lb = LevelBuf{};
+    }
+    tt_free();
+    if (E.scan_status) cudaFree(E.scan_status);
+    if (E.stage) cudaFree(E.stage);
+    cudaFree(E.tickets);
+    cudaFree(E.err);
+    cudaFree(E.plan_dev);
+    cudaFreeHost(E.plan_host);
+    cudaFreeHost(E.host_scratch);
+    cudaEventDestroy(E.ev0);
+    cudaEventDestroy(E.ev1);
+    cudaEventDestroy(E.lev0);
+    cudaEventDestroy(E.lev1);
+    cudaStreamDestroy(E.stream);
+    E.scan_status = nullptr;
+    E.scan_status_cap = 0;
+    E.stage = nullptr;
+    E.stage_cap = 0;
+    E.level_bytes_total = 0;
+    E.ready = false;
+    return PG_OK;
+}
+
+static int op_batch(int op, const pg_board* pos, u32 n, void* out, u32* nout, int slider)
+{
+    Engine& E = engine();
+    const u64 in_bytes = (u64)n * sizeof(Pos);
+    const u64 out_bytes = op == 0 ? (u64)n * 4 : op == 1 ? (u64)n * 512 : (u64)n * 256 * sizeof(Pos);
+    const u64 nbytes = (u64)n * 4;
+    PG_TRY(ensure_stage(in_bytes + out_bytes + nbytes + 64));
+    unsigned char* s = (unsigned char*)E.stage;
+    Pos* d_in = (Pos*)s;
+    void* d_out = s + in_bytes;
+    u32* d_n = (u32*)(s + in_bytes + out_bytes);
+    PG_CUDA(cudaMemcpyAsync(d_in, pos, in_bytes, cudaMemcpyHostToDevice, E.stream));
+    const SliderOps& ops = ops_for(slider);
+    if (op == 0) PG_CUDA(ops.count_batch(d_in, n, (u32*)d_out, E.stream));
+    else if (op == 1) PG_CUDA(ops.gen_moves_batch(d_in, n, (u16*)d_out, d_n, E.stream));
+    else PG_CUDA(ops.gen_boards_batch(d_in, n, (Pos*)d_out, d_n, E.stream));
+    PG_CUDA(cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, E.stream));
+    if (nout) PG_CUDA(cudaMemcpyAsync(nout, d_n, nbytes, cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    return PG_OK;
+}
+
+static int slider_of(int s)
+{
+    if (s == PG_SLIDER_AUTO) s = engine().default_slider;
+    return s == PG_SLIDER_AUTO ? PG_SLIDER_KOGGE_STONE : s;
+}
+
+int pg_count_moves_batch(const pg_board* pos, uint32_t n, uint32_t* out)
+{
+    if (!pos || !out) { set_error("null argument"); return PG_ERR_INVALID_ARGUMENT; }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    if (n == 0) return PG_OK;
+    for (u32 i = 0; i < n; i++)
+        if (!valid_board(pos[i])) { set_error("position %u is not a valid board", i); return PG_ERR_INVALID_POSITION; }
+    return op_batch(0, pos, n, out, nullptr, slider_of(PG_SLIDER_AUTO));
+}
+
+int pg_count_moves(const pg_board* pos, uint32_t* out) { return pg_count_moves_batch(pos, 1, out); }
+
+int pg_generate_moves(const pg_board* pos, pg_move* moves, uint32_t* n)
+{
+    if (!pos || !moves || !n) { set_error("null argument"); return PG_ERR_INVALID_ARGUMENT; }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    if (!valid_board(*pos)) { set_error("not a valid board"); return PG_ERR_INVALID_POSITION; }
+    PG_TRY(op_batch(1, pos, 1, moves, n, slider_of(PG_SLIDER_AUTO)));
+    if (*n > 256) { set_error("more than 256 moves"); return PG_ERR_CAPACITY; }
+    return PG_OK;
+}
+
+int pg_generate_boards(const pg_board* pos, pg_board* out, uint32_t* n)
+{
+    if (!pos || !out || !n) { set_error("null argument"); return PG_ERR_INVALID_ARGUMENT; }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    if (!valid_board(*pos)) { set_error("not a valid board"); return PG_ERR_INVALID_POSITION; }
+    PG_TRY(op_batch(2, pos, 1, out, n, slider_of(PG_SLIDER_AUTO)));
+    if (*n > 256) { set_error("more than 256 boards"); return PG_ERR_CAPACITY; }
+    return PG_OK;
+}
+
+int pg_make_move(pg_board* pos, pg_move move)
+{
+    if (!pos) { set_error("null argument"); return PG_ERR_INVALID_ARGUMENT; }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    PG_TRY(ensure_stage(64));
+    Pos* d = (Pos*)E.stage;
+    u16* dm = (u16*)((unsigned char*)E.stage + 48);
+    PG_CUDA(cudaMemcpyAsync(d, pos, sizeof(Pos), cudaMemcpyHostToDevice, E.stream));
+    PG_CUDA(cudaMemcpyAsync(dm, &move, sizeof(u16), cudaMemcpyHostToDevice, E.stream));
+    PG_CUDA(g_ops_ks.make_batch(d, dm, 1, E.stream));
+    PG_CUDA(cudaMemcpyAsync(pos, d, sizeof(Pos), cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    return PG_OK;
+}
+
+int pg_random_playouts(uint64_t seed, uint32_t n, int min_plies, int max_plies, int min_moves, int depth_lo,
+                       int depth_hi, pg_board* out, uint8_t* depths)
+{
+    if (!out || n == 0 || min_plies < 0 || max_plies < min_plies || depth_hi < depth_lo || depth_lo < 0 || depth_hi > 15) {
+        set_error("bad playout arguments");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    pg_board start;
+    pg_board_from_fen("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1", &start);
+    PG_TRY(ensure_stage((u64)n * 49 + 64));
+    Pos* d = (Pos*)E.stage;
+    unsigned char* dd = (unsigned char*)E.stage + (u64)n * 48;
+    PG_CUDA(cudaMemsetAsync(E.err, 0, 4, E.stream));
+    Pos sp;
+    memcpy(&sp, &start, sizeof(sp));
+    PG_CUDA(g_ops_ks.playouts(sp, seed, n, min_plies, max_plies, std::max(min_moves, 1), depth_lo, depth_hi, d,
+                              depths ? dd : nullptr, E.err, E.stream));
+    PG_CUDA(cudaMemcpyAsync(out, d, (u64)n * 48, cudaMemcpyDeviceToHost, E.stream));
+    if (depths) PG_CUDA(cudaMemcpyAsync(depths, dd, n, cudaMemcpyDeviceToHost, E.stream));
+    return end_call(nullptr);
+}
+
+int pg_perft_batch_device(const pg_board* d_pos, const uint8_t* d_depths, uint32_t n, uint64_t* d_out,
+                          const pg_opts* opts)
+{
+    if (!d_pos || !d_depths || !d_out) { set_error("null argument"); return PG_ERR_INVALID_ARGUMENT; }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    if (n == 0) return PG_OK;
+    PG_TRY(begin_call(opts));
+    if (opts && opts->use_tt) {
+        PG_TRY(tt_perft_batch_device((const Pos*)d_pos, d_depths, n, (u64*)d_out, opts));
+    } else {
+        PG_TRY(perft_batch_device_locked((const Pos*)d_pos, d_depths, n, (u64*)d_out, opts));
+    }
+    return end_call(opts);
+}
+
+int pg_perft_batch(const pg_board* pos, const uint8_t* depths, uint32_t n, uint64_t* out, const pg_opts* opts)
+{
+    if (!pos || !depths || !out) { set_error("null argument"); return PG_ERR_INVALID_ARGUMENT; }
+    Engine& E = engine();
+    std::unique_lock<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    if (n == 0) return PG_OK;
+    for (u32 i = 0; i < n; i++) {
+        if (!valid_board(pos[i])) { set_error("position %u is not a valid board", i); return PG_ERR_INVALID_POSITION; }
+        if (depths[i] > 15) { set_error("depth %u of position %u out of range 0..15", depths[i], i); return PG_ERR_INVALID_ARGUMENT; }
+    }
+    const u64 pb = (u64)n * 48, db = ((u64)n + 15) & ~15ull, ob = (u64)n * 8;
+    PG_TRY(ensure_stage(pb + db + ob + 64));
+    unsigned char* s = (unsigned char*)E.stage;
+    Pos* d_pos = (Pos*)s;
+    unsigned char* d_dep = s + pb;
+    u64* d_out = (u64*)(s + pb + db);
+    PG_TRY(begin_call(opts));
+    PG_CUDA(cudaMemcpyAsync(d_pos, pos, pb, cudaMemcpyHostToDevice, E.stream));
+    PG_CUDA(cudaMemcpyAsync(d_dep, depths, n, cudaMemcpyHostToDevice, E.stream));
+    if (opts && opts->use_tt) {
+        PG_TRY(tt_perft_batch_device(d_pos, d_dep, n, d_out, opts));
+    } else {
+        PG_TRY(perft_batch_device_locked(d_pos, d_dep, n, d_out, opts));
+    }
+    PG_CUDA(cudaMemcpyAsync(out, d_out, ob, cudaMemcpyDeviceToHost, E.stream));
+    PG_TRY(end_call(nullptr));
+    u64 total = 0;
+    for (u32 i = 0; i < n; i++) total += out[i];
+    E.st.leaves = total;
+    if (opts && opts->stats) *opts->stats = E.st;
+    return PG_OK;
+}
+
+int pg_perft(const pg_board* pos, int depth, uint64_t* out, const pg_opts* opts)
+{
+    if (!pos || !out || depth < 0 || depth > 15) { set_error("bad argument"); return PG_ERR_INVALID_ARGUMENT; }
+    const uint8_t d = (uint8_t)depth;
+    return pg_perft_batch(pos, &d, 1, out, opts);
+}
+
+int pg_perft_divide(const pg_board* pos, int depth, pg_move* moves, uint64_t* counts, uint32_t* n,
+                    const pg_opts* opts)
+{
+    if (!pos || !moves || !counts || !n || depth < 1 || depth > 15) {
+        set_error("bad argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    PG_TRY(pg_generate_moves(pos, moves, n));
+    if (*n == 0) return PG_OK;
+    pg_board kids[256];
+    {
+        Engine& E = engine();
+        std::lock_guard<std::mutex> lk(E.mu);
+        PG_TRY(ensure_stage(256 * 48 + 512 + 64));
+        Pos* d = (Pos*)E.stage;
+        u16* dm = (u16*)((unsigned char*)E.stage + 256 * 48);
+        for (u32 i = 0; i < *n; i++) kids[i] = *pos;
+        PG_CUDA(cudaMemcpyAsync(d, kids, *n * 48, cudaMemcpyHostToDevice, E.stream));
+        PG_CUDA(cudaMemcpyAsync(dm, moves, *n * 2, cudaMemcpyHostToDevice, E.stream));
+        PG_CUDA(g_ops_ks.make_batch(d, dm, *n, E.stream));
+        PG_CUDA(cudaMemcpyAsync(kids, d, *n * 48, cudaMemcpyDeviceToHost, E.stream));
+        PG_CUDA(cudaStreamSynchronize(E.stream));
+    }
+    uint8_t dep[256];
+    for (u32 i = 0; i < *n; i++) dep[i] = (uint8_t)(depth - 1);
+    return pg_perft_batch(kids, dep, *n, counts, opts);
+}
+
+}  // extern "C"

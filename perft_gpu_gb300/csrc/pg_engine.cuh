@@ -1,0 +1,87 @@
+// pg_engine.cuh -- engine state shared by the translation units of the
+// library (host side) and the kernel interfaces they launch.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/perft_gb300.h"
+#include "pg_board.cuh"
+
+namespace pg {
+
+constexpr int MAX_LEVELS = 16;
+constexpr u32 MAX_CHUNKS = 2048;      // greedy chunks planned per expansion
+constexpr u32 MAX_TICKETS = 1 << 16;  // dynamic-scheduling counters per call
+
+// device error bits (bounded waits and capacity guards set them; no trap)
+enum : u32 {
+    ERR_SCAN_TIMEOUT = 1u << 0,
+    ERR_PLAN_OVERFLOW = 1u << 1,
+    ERR_PLAYOUT_ATTEMPTS = 1u << 2,
+    ERR_QUEUE_MISMATCH = 1u << 3,
+    ERR_GRID_BARRIER_TIMEOUT = 1u << 4,
+    ERR_TT_GUARD = 1u << 5,
+};
+
+// one frontier level in HBM: boards as three 16-byte planes (struct of
+// arrays, one ulonglong2 per board per plane), group id and remaining depth
+struct LevelView {
+    ulonglong2* pl0;  // (white, pawns)
+    ulonglong2* pl1;  // (knights, bishop_queens)
+    ulonglong2* pl2;  // (rook_queens, kings)
+    u32* grp;
+    unsigned char* rem;
+};
+
+struct LevelBuf {
+    LevelView v{};
+    u32* cnt = nullptr;   // children per node (0 for leaf-handled nodes)
+    u64* offs = nullptr;  // exclusive scan of cnt, cap + 1 entries
+    u64 cap = 0;
+    void* block = nullptr;
+};
+
+struct PlanOut {
+    u32 nchunks;
+    u32 pad;
+    u64 total;
+    u32 bnd[MAX_CHUNKS + 1];
+    u64 coff[MAX_CHUNKS + 1];  // offs[] at each boundary
+};
+
+struct Engine {
+    std::mutex mu;
+    bool ready = false;
+    int device = 0;
+    int num_sms = 0;
+    int verbose = 0;
+    int default_slider = PG_SLIDER_AUTO;
+    u64 budget = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, lev0 = nullptr, lev1 = nullptr;
+    LevelBuf lv[MAX_LEVELS];
+    u64 level_bytes_total = 0;
+    // scratch
+    u64* scan_status = nullptr;
+    u64 scan_status_cap = 0;
+    u32* tickets = nullptr;  // MAX_TICKETS counters, zeroed per call
+    u32 ticket_next = 0;
+    u32* err = nullptr;
+    PlanOut* plan_dev = nullptr;
+    PlanOut* plan_host = nullptr;  // pinned
+    u64* acc = nullptr;            // per-group counters
+    u64 acc_cap = 0;
+    void* stage = nullptr;         // staging for host-array calls
+    u64 stage_cap = 0;
+    u64* host_scratch = nullptr;   // pinned small scratch
+    // statistics of the current call
+    pg_stats st{};
+};
+
+Engine& engine();
+void set_error(const char* fmt, ...);
+
+}  // namespace pg

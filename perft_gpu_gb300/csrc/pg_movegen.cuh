@@ -1,0 +1,836 @@
+// pg_movegen.cuh -- legal move generation for sm_103a, side-templated.
+//
+// Semantics follow the reference's MoveGeneratorBitboard (MGB.h below):
+//   count_moves    <- countMoves<c>          MGB.h:3008-3295 (+2825-3002)
+//   gen_moves      <- generateMoves<c>       MGB.h:2469-2823 (+2266-2463),
+//                     host flavour (capture flag on non-pawn captures outside
+//                     check, MGB.h:2525-2529); same order, same flags
+//   make_move      <- makeMove<c,false>      MGB.h:3310-3570 with exact
+//                     en-passant flagging (MGB.h:3528-3547)
+//   gen_boards     <- generateBoards<c>      MGB.h:1940-2261 (+1741-1933,
+//                     child boards as built by MGB.h:1302-1738)
+// The legality rules are the reference's, including its behaviour on
+// castling rights without a rook (no rook test) and on en passant while in
+// check (only when the captured pawn is the checker).
+//
+// The formulation is our own and built for a 32-bit SIMT ALU: no per-thread
+// colour branches (S is a template parameter and frontier ranges are
+// side-uniform), own slider moves counted set-wise per direction with the
+// Kogge-Stone policy (rays of different sliders along one direction are
+// disjoint, so the popcounts add up exactly), and pins found from the king's
+// four lines without lookup tables.
+#pragma once
+#include "pg_board.cuh"
+#include "pg_tables.h"
+
+namespace pg {
+
+// ---------------------------------------------------------------------------
+// slider attack policies
+// ---------------------------------------------------------------------------
+
+// Every translation unit that includes this header owns one copy of the
+// tables (non-relocatable device code gives __device__ variables internal
+// linkage) and uploads it through its own upload function at pg_init.
+static __device__ MagicSq g_magic_rook[64];
+static __device__ MagicSq g_magic_bishop[64];
+static __device__ u64 g_magic_attacks[MAGIC_TABLE_ENTRIES];
+static __device__ __align__(16) unsigned char g_magic_bytes[MAGIC_TABLE_ENTRIES];
+static __device__ u64 g_magic_unique[UNIQUE_TOTAL];
+static __device__ u64 g_knight[64];
+
+// Kogge-Stone: pure shift/and/or, no memory traffic.
+struct SlKS {
+    static constexpr int kId = 0;
+    static constexpr bool kSetwise = true;
+    __device__ __forceinline__ static u64 bishop(int sq, u64 occ) { return ks_bishop(1ull << sq, ~occ); }
+    __device__ __forceinline__ static u64 rook(int sq, u64 occ) { return ks_rook(1ull << sq, ~occ); }
+};
+
+// fancy magics, 841 KB attack table read through the L1/L2 (ld.global.nc)
+struct SlFancy {
+    static constexpr int kId = 1;
+    static constexpr bool kSetwise = false;
+    __device__ __forceinline__ static u64 look(const MagicSq* t, int sq, u64 occ)
+    {
+        const u64 mask = __ldg(&t[sq].mask), magic = __ldg(&t[sq].magic);
+        const u32 off = __ldg(&t[sq].offset), sh = __ldg(&t[sq].shift);
+        return __ldg(&g_magic_attacks[off + (u32)(((occ & mask) * magic) >> sh)]);
+    }
+    __device__ __forceinline__ static u64 bishop(int sq, u64 occ) { return look(g_magic_bishop, sq, occ); }
+    __device__ __forceinline__ static u64 rook(int sq, u64 occ) { return look(g_magic_rook, sq, occ); }
+};
+
+// byte-lookup fancy magics staged in shared memory (158 KB per CTA): the hash
+// selects a byte, the byte selects one of the square's unique attack sets.
+struct SmemTables {
+    u64 unique[UNIQUE_TOTAL];
+    MagicSq rook[64];
+    MagicSq bishop[64];
+    unsigned char bytes[MAGIC_TABLE_ENTRIES];
+};
+constexpr int SMEM_TABLE_BYTES = (int)sizeof(SmemTables);
+
+struct SlByteSmem {
+    static constexpr int kId = 2;
+    static constexpr bool kSetwise = false;
+    __device__ __forceinline__ static SmemTables* tab()
+    {
+        extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
+        return reinterpret_cast<SmemTables*>(pg_dyn_smem);
+    }
+    __device__ __forceinline__ static u64 look(const MagicSq& e, int sq, u64 occ)
+    {
+        const SmemTables* t = tab();
+        u32 idx = e.offset + (u32)(((occ & e.mask) * e.magic) >> e.shift);
+        return t->unique[e.uniq + t->bytes[idx]];
+    }
+    __device__ __forceinline__ static u64 bishop(int sq, u64 occ) { return look(tab()->bishop[sq], sq, occ); }
+    __device__ __forceinline__ static u64 rook(int sq, u64 occ) { return look(tab()->rook[sq], sq, occ); }
+    // every thread of the CTA calls this once before the first lookup
+    __device__ static void stage()
+    {
+        SmemTables* t = tab();
+        const int tid = threadIdx.x, nt = blockDim.x;
+        const uint4* src_b = reinterpret_cast<const uint4*>(g_magic_bytes);
+        uint4* dst_b = reinterpret_cast<uint4*>(t->bytes);
+        for (int i = tid; i < MAGIC_TABLE_ENTRIES / 16; i += nt) dst_b[i] = __ldg(&src_b[i]);
+        for (int i = tid; i < UNIQUE_TOTAL; i += nt) t->unique[i] = __ldg(&g_magic_unique[i]);
+        for (int i = tid; i < 64; i += nt) {
+            t->rook[i] = g_magic_rook[i];
+            t->bishop[i] = g_magic_bishop[i];
+        }
+        __syncthreads();
+    }
+};
+
+template <class SL> __device__ __forceinline__ void stage_tables()
+{
+    if constexpr (SL::kId == 2) SlByteSmem::stage();
+}
+template <class SL> constexpr int table_smem_bytes() { return SL::kId == 2 ? SMEM_TABLE_BYTES : 0; }
+
+template <class SL> __device__ __forceinline__ u64 bishops_of(u64 set, u64 occ)
+{
+    if constexpr (SL::kSetwise) {
+        return ks_bishop(set, ~occ);
+    } else {
+        u64 a = 0;
+        for (; set; set &= set - 1) a |= SL::bishop(lsb(set), occ);
+        return a;
+    }
+}
+template <class SL> __device__ __forceinline__ u64 rooks_of(u64 set, u64 occ)
+{
+    if constexpr (SL::kSetwise) {
+        return ks_rook(set, ~occ);
+    } else {
+        u64 a = 0;
+        for (; set; set &= set - 1) a |= SL::rook(lsb(set), occ);
+        return a;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-position facts
+// ---------------------------------------------------------------------------
+
+template <int S> struct Sides {
+    u64 pawns, occ, mine, theirs, king, tbq, trq;
+    int ksq;
+    __device__ __forceinline__ explicit Sides(const Pos& b)
+    {
+        pawns = b.p & INNER;
+        occ = b.k | pawns | b.n | b.bq | b.rq;
+        const u64 black = occ & ~b.w;
+        mine = S ? black : b.w;
+        theirs = S ? b.w : black;
+        king = b.k & mine;
+        ksq = lsb(king) & 63;
+        tbq = b.bq & theirs;
+        trq = b.rq & theirs;
+    }
+};
+
+// findPinnedPieces (MGB.h:1213-1249): the single piece between the king and
+// an aligned enemy slider.  Aligned sliders are taken from the king's four
+// lines, and the squares between from the line and the index range.
+__device__ __forceinline__ u64 find_pinned(int ksq, u64 tbq, u64 trq, u64 occ)
+{
+    const u64 kb = 1ull << ksq;
+    const u64 lf = file_of(ksq), lr = rank_of(ksq), ld = diag_of(ksq), la = anti_of(ksq);
+    u64 cand = (((lf | lr) & trq) | ((ld | la) & tbq)) & ~kb;
+    u64 pinned = 0;
+    while (cand) {
+        const int a = lsb(cand);
+        const u64 ab = 1ull << a;
+        const u64 line = (lf & ab) ? lf : (lr & ab) ? lr : (ld & ab) ? ld : la;
+        const u64 inb = between_on(line, a, ksq) & occ;
+        if (!several(inb)) pinned |= inb;
+        cand &= cand - 1;
+    }
+    return pinned;
+}
+
+// the line through the king that holds square bit sb (0 when none)
+__device__ __forceinline__ u64 king_line(int ksq, u64 sb)
+{
+    const u64 lf = file_of(ksq), lr = rank_of(ksq), ld = diag_of(ksq), la = anti_of(ksq);
+    return (lf & sb) ? lf : (lr & sb) ? lr : (ld & sb) ? ld : (la & sb) ? la : 0ull;
+}
+
+// findAttackedSquares (MGB.h:1254-1298) with the own king removed
+template <int S, class SL> __device__ __forceinline__ u64 threat_full(const Pos& b, const Sides<S>& c)
+{
+    const u64 occ_nk = c.occ & ~c.king;
+    u64 t = pawn_attacks<1 - S>(c.pawns & c.theirs);
+    t |= knight_set(b.n & c.theirs);
+    t |= king_set(b.k & c.theirs);
+    t |= bishops_of<SL>(c.tbq, occ_nk);
+    t |= rooks_of<SL>(c.trq, occ_nk);
+    return t;
+}
+
+template <int S> __device__ __forceinline__ u64 ep_target(const Pos& b)
+{
+    const int ep = st_ep(b);
+    return ep ? ((1ull << (ep - 1)) << (S ? 16 : 40)) : 0ull;
+}
+
+template <int S> __device__ __forceinline__ bool can_castle_k(const Pos& b, u64 occ, u64 threat)
+{
+    if (S == 0) return (st_wc(b) & 1) && !(W_KS_PATH & occ) && !(W_KS_PATH & threat);
+    return (st_bc(b) & 1) && !(B_KS_PATH & occ) && !(B_KS_PATH & threat);
+}
+template <int S> __device__ __forceinline__ bool can_castle_q(const Pos& b, u64 occ, u64 threat)
+{
+    if (S == 0) return (st_wc(b) & 2) && !(W_QS_PATH & occ) && !(W_QS_SAFE & threat);
+    return (st_bc(b) & 2) && !(B_QS_PATH & occ) && !(B_QS_SAFE & threat);
+}
+
+// en passant outside check (MGB.h:3058-3093): a pinned capturer must stay on
+// its pin line; otherwise the rank of the two pawns must not open onto the king
+template <int S> __device__ __forceinline__ bool ep_legal(const Sides<S>& c, u64 pinned, u64 pawn, u64 tgt, u64 victim)
+{
+    if (pawn & pinned) return (tgt & king_line(c.ksq, pawn)) != 0;
+    const u64 pro = ~c.occ | victim | pawn;
+    return ((ray<1, true>(c.trq, pro) | ray<1, false>(c.trq, pro)) & c.king) == 0;
+}
+
+// checkers of the king (MGB.h:2842-2860)
+template <int S, class SL> __device__ __forceinline__ u64 checkers(const Pos& b, const Sides<S>& c)
+{
+    u64 a = pawn_attackers_of<S>(c.king) & (c.pawns & c.theirs);
+    a |= knight_set(c.king) & (b.n & c.theirs);
+    a |= SL::bishop(c.ksq, c.occ) & c.tbq;
+    a |= SL::rook(c.ksq, c.occ) & c.trq;
+    return a;
+}
+
+// ---------------------------------------------------------------------------
+// countMoves
+// ---------------------------------------------------------------------------
+
+// countMovesOutOfCheck (MGB.h:2825-3002); counted set-wise where the
+// per-piece sums are provably equal.
+template <int S, class SL>
+__device__ __noinline__ u32 count_evasions(const Pos& b)
+{
+    const Sides<S> c(b);
+    const u64 threat = threat_full<S, SL>(b, c);
+    u32 n = popc(king_set(c.king) & ~(threat | c.mine));
+    const u64 att = checkers<S, SL>(b, c);
+    if (!att || several(att)) return n;
+    const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
+    const int asq = lsb(att);
+    const u64 safe = att | between_on(king_line(c.ksq, att), asq, c.ksq);
+    const u64 mine = c.mine & ~pinned;
+    const u64 empty = ~c.occ;
+    const u64 P = c.pawns & mine;
+    // pushes: a safe single push (4 if promotion); otherwise a safe double push
+    const u64 d1 = push1<S>(P) & empty;
+    n += popc(d1 & safe) + 3 * popc(d1 & safe & BACK_RANKS);
+    n += popc(push1<S>(d1 & ~safe & double_rank<S>()) & safe & empty);
+    // captures of the checker
+    const u64 hitw = cap_w<S>(P) & c.theirs & safe, hite = cap_e<S>(P) & c.theirs & safe;
+    n += (popc(hitw) + popc(hite)) * ((att & BACK_RANKS) ? 4 : 1);
+    // en passant only when the double-pushed pawn is the checker
+    u64 tgt = ep_target<S>(b);
+    const u64 victim = S ? up(tgt) : down(tgt);
+    if (victim != att) tgt = 0;
+    n += popc(cap_w<S>(P) & tgt) + popc(cap_e<S>(P) & tgt);
+    for (u64 s = b.n & mine; s; s &= s - 1) n += popc(knight_set(lowbit(s)) & safe);
+    for (u64 s = b.bq & mine; s; s &= s - 1) n += popc(SL::bishop(lsb(s), c.occ) & safe);
+    for (u64 s = b.rq & mine; s; s &= s - 1) n += popc(SL::rook(lsb(s), c.occ) & safe);
+    return n;
+}
+
+// pinned pawns and en passant outside check (rare; kept out of line)
+template <int S>
+__device__ __noinline__ u32 count_pawn_specials(const Pos& b, u64 pinned)
+{
+    const Sides<S> c(b);
+    const u64 myp = c.pawns & c.mine;
+    u32 n = 0;
+    const u64 tgt = ep_target<S>(b);
+    if (tgt) {
+        const u64 victim = S ? up(tgt) : down(tgt);
+        for (u64 s = (east1(victim) | west1(victim)) & myp; s; s &= s - 1)
+            n += ep_legal<S>(c, pinned, lowbit(s), tgt, victim) ? 1 : 0;
+    }
+    for (u64 s = myp & pinned; s; s &= s - 1) {
+        const u64 p = lowbit(s);
+        const u64 line = king_line(c.ksq, p);
+        const u64 d = push1<S>(p) & line & ~c.occ;
+        if (d) {
+            n++;
+            if (push1<S>(d & double_rank<S>()) & ~c.occ) n++;
+        }
+        const u64 x = (cap_w<S>(p) & line) | (cap_e<S>(p) & line);
+        if (x & c.theirs) n += (x & BACK_RANKS) ? 4 : 1;
+    }
+    return n;
+}
+
+// countMoves (MGB.h:3008-3295)
+template <int S, class SL>
+__device__ __forceinline__ u32 count_moves(const Pos& b)
+{
+    const Sides<S> c(b);
+    const u64 empty = ~c.occ;
+    const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
+    const u64 my_bq = b.bq & c.mine, my_rq = b.rq & c.mine;
+
+    // enemy attacks.  Outside check no enemy ray reaches the king, so the
+    // rays through the king's square need not be extended; in check the
+    // evasion path recomputes them with the king removed.
+    u64 threat = pawn_attacks<1 - S>(c.pawns & c.theirs) | knight_set(b.n & c.theirs) | king_set(b.k & c.theirs);
+    u32 n = 0;
+    if constexpr (SL::kSetwise) {
+        // own sliders split by the one line they may still move along
+        const u64 pl = pinned & c.mine;
+        const u64 ns = my_rq & ~(pl & ~file_of(c.ksq));
+        const u64 ew = my_rq & ~(pl & ~rank_of(c.ksq));
+        const u64 dg = my_bq & ~(pl & ~diag_of(c.ksq));
+        const u64 ad = my_bq & ~(pl & ~anti_of(c.ksq));
+        const u64 tgt_mask = ~c.mine;
+        {
+            const Pro<8, true> pr(empty);
+            threat |= pr.attacks(c.trq);
+            n += popc(pr.attacks(ns) & tgt_mask);
+        }
+        {
+            const Pro<8, false> pr(empty);
+            threat |= pr.attacks(c.trq);
+            n += popc(pr.attacks(ns) & tgt_mask);
+        }
+        {
+            const Pro<1, true> pr(empty);
+            threat |= pr.attacks(c.trq);
+            n += popc(pr.attacks(ew) & tgt_mask);
+        }
+        {
+            const Pro<1, false> pr(empty);
+            threat |= pr.attacks(c.trq);
+            n += popc(pr.attacks(ew) & tgt_mask);
+        }
+        {
+            const Pro<9, true> pr(empty);
+            threat |= pr.attacks(c.tbq);
+            n += popc(pr.attacks(dg) & tgt_mask);
+        }
+        {
+            const Pro<9, false> pr(empty);
+            threat |= pr.attacks(c.tbq);
+            n += popc(pr.attacks(dg) & tgt_mask);
+        }
+        {
+            const Pro<7, true> pr(empty);
+            threat |= pr.attacks(c.tbq);
+            n += popc(pr.attacks(ad) & tgt_mask);
+        }
+        {
+            const Pro<7, false> pr(empty);
+            threat |= pr.attacks(c.tbq);
+            n += popc(pr.attacks(ad) & tgt_mask);
+        }
+        if (threat & c.king) return count_evasions<S, SL>(b);
+    } else {
+        threat |= bishops_of<SL>(c.tbq, c.occ) | rooks_of<SL>(c.trq, c.occ);
+        if (threat & c.king) return count_evasions<S, SL>(b);
+        for (u64 s = my_bq; s; s &= s - 1) {
+            const int sq = lsb(s);
+            u64 m = SL::bishop(sq, c.occ) & ~c.mine;
+            if (pinned & (1ull << sq)) m &= king_line(c.ksq, 1ull << sq);
+            n += popc(m);
+        }
+        for (u64 s = my_rq; s; s &= s - 1) {
+            const int sq = lsb(s);
+            u64 m = SL::rook(sq, c.occ) & ~c.mine;
+            if (pinned & (1ull << sq)) m &= king_line(c.ksq, 1ull << sq);
+            n += popc(m);
+        }
+    }
+
+    const u64 myp = c.pawns & c.mine;
+    if ((myp & pinned) | (b.p & 0xF0ull)) n += count_pawn_specials<S>(b, pinned);
+    const u64 fp = myp & ~pinned;
+    const u64 d1 = push1<S>(fp) & empty;
+    n += popc(d1) + 3 * popc(d1 & BACK_RANKS);
+    n += popc(push1<S>(d1 & double_rank<S>()) & empty);
+    const u64 cw = cap_w<S>(fp) & c.theirs, ce = cap_e<S>(fp) & c.theirs;
+    n += popc(cw) + popc(ce) + 3 * (popc(cw & BACK_RANKS) + popc(ce & BACK_RANKS));
+    n += can_castle_k<S>(b, c.occ, threat) + can_castle_q<S>(b, c.occ, threat);
+    n += popc(king_set(c.king) & ~(threat | c.mine));
+    for (u64 s = b.n & c.mine & ~pinned; s; s &= s - 1) n += popc(__ldg(&g_knight[lsb(s)]) & ~c.mine);
+    return n;
+}
+
+// ---------------------------------------------------------------------------
+// generateMoves (reference order, host flags)
+// ---------------------------------------------------------------------------
+
+// addCompactPawnMoves (MGB.h:1717-1738): promotions N, B, Q, R
+template <class E> __device__ __forceinline__ void emit_pawn(E& emit, int from, u64 dst, int fl)
+{
+    const int to = lsb(dst);
+    if (dst & BACK_RANKS) {
+        emit(cmove(from, to, fl | MF_PROMO_N));
+        emit(cmove(from, to, fl | MF_PROMO_B));
+        emit(cmove(from, to, fl | MF_PROMO_Q));
+        emit(cmove(from, to, fl | MF_PROMO_R));
+    } else {
+        emit(cmove(from, to, fl));
+    }
+}
+
+// generateMovesOutOfCheck (MGB.h:2266-2463)
+template <int S, class SL, class E>
+__device__ __noinline__ void gen_evasions(const Pos& b, E& emit)
+{
+    const Sides<S> c(b);
+    const u64 threat = threat_full<S, SL>(b, c);
+    for (u64 s = king_set(c.king) & ~(threat | c.mine); s; s &= s - 1) emit(cmove(c.ksq, lsb(s), 0));
+    const u64 att = checkers<S, SL>(b, c);
+    if (!att || several(att)) return;
+    const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
+    const u64 safe = att | between_on(king_line(c.ksq, att), lsb(att), c.ksq);
+    const u64 mine = c.mine & ~pinned;
+    u64 tgt = ep_target<S>(b);
+    const u64 victim = S ? up(tgt) : down(tgt);
+    if (victim != att) tgt = 0;
+    for (u64 pw = c.pawns & mine; pw; pw &= pw - 1) {
+        const u64 p = lowbit(pw);
+        const int from = lsb(p);
+        const u64 d = push1<S>(p) & ~c.occ;
+        if (d) {
+            if (d & safe) {
+                emit_pawn(emit, from, d, 0);
+            } else {
+                const u64 d2 = push1<S>(d & double_rank<S>()) & safe & ~c.occ;
+                if (d2) emit(cmove(from, lsb(d2), MF_DOUBLE));
+            }
+        }
+        const u64 caps = cap_w<S>(p) | cap_e<S>(p);
+        const u64 hit = caps & c.theirs & safe;
+        if (hit) emit_pawn(emit, from, hit, MF_CAPTURE);
+        const u64 epd = caps & tgt;
+        if (epd) emit(cmove(from, lsb(epd), MF_EP));
+    }
+    for (u64 s = b.n & mine; s; s &= s - 1)
+        for (u64 m = __ldg(&g_knight[lsb(s)]) & safe; m; m &= m - 1) emit(cmove(lsb(s), lsb(m), 0));
+    for (u64 s = b.bq & mine; s; s &= s - 1)
+        for (u64 m = SL::bishop(lsb(s), c.occ) & safe; m; m &= m - 1) emit(cmove(lsb(s), lsb(m), 0));
+    for (u64 s = b.rq & mine; s; s &= s - 1)
+        for (u64 m = SL::rook(lsb(s), c.occ) & safe; m; m &= m - 1) emit(cmove(lsb(s), lsb(m), 0));
+}
+
+template <int S, class SL, class E>
+__device__ __forceinline__ void gen_moves(const Pos& b, E& emit)
+{
+    const Sides<S> c(b);
+    const u64 threat = threat_full<S, SL>(b, c);
+    if (threat & c.king) {
+        gen_evasions<S, SL>(b, emit);
+        return;
+    }
+    const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
+    auto capf = [&](u64 m) { return (lowbit(m) & c.theirs) ? MF_CAPTURE : 0; };
+    for (u64 s = king_set(c.king) & ~(threat | c.mine); s; s &= s - 1) emit(cmove(c.ksq, lsb(s), capf(s)));
+    for (u64 s = b.n & c.mine & ~pinned; s; s &= s - 1)
+        for (u64 m = __ldg(&g_knight[lsb(s)]) & ~c.mine; m; m &= m - 1) emit(cmove(lsb(s), lsb(m), capf(m)));
+    const u64 my_bq = b.bq & c.mine, my_rq = b.rq & c.mine;
+    for (u64 s = my_bq & pinned; s; s &= s - 1)
+        for (u64 m = SL::bishop(lsb(s), c.occ) & ~c.mine & king_line(c.ksq, lowbit(s)); m; m &= m - 1)
+            emit(cmove(lsb(s), lsb(m), capf(m)));
+    for (u64 s = my_bq & ~pinned; s; s &= s - 1)
+        for (u64 m = SL::bishop(lsb(s), c.occ) & ~c.mine; m; m &= m - 1) emit(cmove(lsb(s), lsb(m), capf(m)));
+    for (u64 s = my_rq & pinned; s; s &= s - 1)
+        for (u64 m = SL::rook(lsb(s), c.occ) & ~c.mine & king_line(c.ksq, lowbit(s)); m; m &= m - 1)
+            emit(cmove(lsb(s), lsb(m), capf(m)));
+    for (u64 s = my_rq & ~pinned; s; s &= s - 1)
+        for (u64 m = SL::rook(lsb(s), c.occ) & ~c.mine; m; m &= m - 1) emit(cmove(lsb(s), lsb(m), capf(m)));
+    const u64 myp = c.pawns & c.mine;
+    const u64 tgt = ep_target<S>(b);
+    if (tgt) {
+        const u64 victim = S ? up(tgt) : down(tgt);
+        for (u64 s = (east1(victim) | west1(victim)) & myp; s; s &= s - 1)
+            if (ep_legal<S>(c, pinned, lowbit(s), tgt, victim)) emit(cmove(lsb(s), lsb(tgt), MF_EP));
+    }
+    for (u64 s = myp & pinned; s; s &= s - 1) {
+        const u64 p = lowbit(s);
+        const int from = lsb(p);
+        const u64 line = king_line(c.ksq, p);
+        const u64 d = push1<S>(p) & line & ~c.occ;
+        if (d) {
+            emit(cmove(from, lsb(d), 0));
+            const u64 d2 = push1<S>(d & double_rank<S>()) & ~c.occ;
+            if (d2) emit(cmove(from, lsb(d2), MF_DOUBLE));
+        }
+        const u64 x = (cap_w<S>(p) & line) | (cap_e<S>(p) & line);
+        if (x & c.theirs) emit_pawn(emit, from, x, MF_CAPTURE);
+    }
+    for (u64 s = myp & ~pinned; s; s &= s - 1) {
+        const u64 p = lowbit(s);
+        const int from = lsb(p);
+        const u64 d = push1<S>(p) & ~c.occ;
+        if (d) {
+            emit_pawn(emit, from, d, 0);
+            const u64 d2 = push1<S>(d & double_rank<S>()) & ~c.occ;
+            if (d2) emit_pawn(emit, from, d2, MF_DOUBLE);
+        }
+        const u64 w = cap_w<S>(p) & c.theirs;
+        if (w) emit_pawn(emit, from, w, MF_CAPTURE);
+        const u64 e = cap_e<S>(p) & c.theirs;
+        if (e) emit_pawn(emit, from, e, MF_CAPTURE);
+    }
+    if (can_castle_k<S>(b, c.occ, threat)) emit(cmove(S ? 60 : 4, S ? 62 : 6, MF_KCASTLE));
+    if (can_castle_q<S>(b, c.occ, threat)) emit(cmove(S ? 60 : 4, S ? 58 : 2, MF_QCASTLE));
+}
+
+// ---------------------------------------------------------------------------
+// makeMove
+// ---------------------------------------------------------------------------
+
+// updateCastleFlag (MGB.h:1302-1340)
+__device__ __forceinline__ void castle_update(Pos& b, u64 sq, int mover)
+{
+    if (mover == 0) {
+        if (sq & (1ull << 63)) set_bc(b, st_bc(b) & ~1);
+        else if (sq & (1ull << 56)) set_bc(b, st_bc(b) & ~2);
+    } else {
+        if (sq & (1ull << 7)) set_wc(b, st_wc(b) & ~1);
+        else if (sq & 1ull) set_wc(b, st_wc(b) & ~2);
+    }
+}
+
+// makeMove<c,false> (MGB.h:3310-3570), en-passant file set only when an enemy
+// pawn stands beside the pushed pawn (MGB.h:3528-3547)
+template <int S>
+__device__ __forceinline__ void make_move(Pos& b, u16 mv)
+{
+    const int from = mv & 63, to = (mv >> 6) & 63, fl = (mv >> 12) & 15;
+    const u64 src = 1ull << from, dst = 1ull << to;
+    // moving piece: K, N, P, Q, B else R; a promotion flag overrides
+    const bool isK = b.k & src, isN = b.n & src, isP = (b.p & INNER) & src;
+    const bool isB0 = b.bq & src, isR0 = b.rq & src;
+    bool toN, toB, toR, toP;
+    if (fl & 8) {
+        const int pr = fl & 3;  // 0 N, 1 B, 2 R, 3 Q
+        toN = pr == 0;
+        toB = pr == 1 || pr == 3;
+        toR = pr >= 2;
+        toP = false;
+    } else {
+        toN = isN && !isK;
+        toP = isP && !isK && !isN;
+        const bool slider = !isK && !isN && !isP;
+        toB = slider && isB0;                     // bishop or queen
+        toR = slider && (isR0 || !isB0);          // rook, queen, or nothing
+    }
+    const bool pieceIsRook = (fl & 8) ? ((fl & 3) == 2) : (!isK && !isN && !isP && !(isB0 && isR0) && !isB0);
+    const u64 clr = ~(src | dst);
+    b.bq &= clr;
+    b.rq &= clr;
+    b.k &= clr;
+    b.n &= clr;
+    b.p &= ~((src | dst) & INNER);
+    if (isK && !(fl & 8)) {
+        b.k |= dst;
+        if (S) set_bc(b, 0); else set_wc(b, 0);
+    }
+    if (toN) b.n |= dst;
+    if (toP) b.p |= dst;
+    if (toB) b.bq |= dst;
+    if (toR) b.rq |= dst;
+    b.w = S ? (b.w & ~dst) : ((b.w ^ src) | dst);
+    if (fl == MF_EP) {
+        const u64 victim = S ? up(dst) : down(dst);
+        b.p &= ~(victim & INNER);
+        if (S) b.w &= ~victim;
+    }
+    if (fl == MF_KCASTLE || fl == MF_QCASTLE) {
+        const int base = S ? 56 : 0;
+        const u64 rf = 1ull << (base + (fl == MF_KCASTLE ? 7 : 0));
+        const u64 rt = 1ull << (base + (fl == MF_KCASTLE ? 5 : 3));
+        b.rq = (b.rq ^ rf) | rt;
+        if (!S) b.w = (b.w ^ rf) | rt;
+    }
+    set_side(b, 1 - S);
+    set_ep(b, 0);
+    castle_update(b, dst, S);
+    if (pieceIsRook) castle_update(b, src, 1 - S);
+    if (fl == MF_DOUBLE) {
+        const u64 pawns = b.p & INNER;
+        const u64 occ = b.k | pawns | b.n | b.bq | b.rq;
+        const u64 enemy = S ? b.w : (occ & ~b.w);
+        if ((east1(dst) | west1(dst)) & pawns & enemy) set_ep(b, (from & 7) + 1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// generateBoards (reference order, reference child-board bytes)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ u64 new_white(const Pos& b, int S, u64 src, u64 dst)
+{
+    return S ? (b.w & ~dst) : ((b.w ^ src) | dst);
+}
+
+// addSlidingMove (MGB.h:1342-1397)
+template <int S, class E> __device__ __forceinline__ void bd_slider(E& emit, const Pos& b, u64 src, u64 dst)
+{
+    Pos nb;
+    nb.bq = b.bq & ~dst;
+    nb.rq = b.rq & ~dst;
+    nb.k = b.k & ~dst;
+    nb.n = b.n & ~dst;
+    nb.p = b.p & ~(dst & INNER);
+    const u64 isb = nb.bq & src, isr = nb.rq & src;
+    nb.bq ^= isb;
+    nb.rq ^= isr;
+    if (isb) nb.bq |= dst;
+    if (isr) nb.rq |= dst;
+    nb.w = new_white(b, S, src, dst);
+    set_side(nb, 1 - S);
+    set_ep(nb, 0);
+    castle_update(nb, dst, S);
+    castle_update(nb, src, 1 - S);
+    emit(nb);
+}
+// addKnightMove (MGB.h:1400-1438)
+template <int S, class E> __device__ __forceinline__ void bd_knight(E& emit, const Pos& b, u64 src, u64 dst)
+{
+    Pos nb;
+    nb.bq = b.bq & ~dst;
+    nb.rq = b.rq & ~dst;
+    nb.k = b.k & ~dst;
+    nb.p = b.p & ~(dst & INNER);
+    nb.n = (b.n ^ src) | dst;
+    nb.w = new_white(b, S, src, dst);
+    set_side(nb, 1 - S);
+    set_ep(nb, 0);
+    castle_update(nb, dst, S);
+    emit(nb);
+}
+// addKingMove (MGB.h:1441-1484)
+template <int S, class E> __device__ __forceinline__ void bd_king(E& emit, const Pos& b, u64 src, u64 dst)
+{
+    Pos nb;
+    nb.bq = b.bq & ~dst;
+    nb.rq = b.rq & ~dst;
+    nb.n = b.n & ~dst;
+    nb.p = b.p & ~(dst & INNER);
+    nb.k = (b.k ^ src) | dst;
+    nb.w = new_white(b, S, src, dst);
+    if (S) set_bc(nb, 0); else set_wc(nb, 0);
+    set_side(nb, 1 - S);
+    set_ep(nb, 0);
+    castle_update(nb, dst, S);
+    emit(nb);
+}
+// addCastleMove (MGB.h:1487-1522)
+template <int S, class E> __device__ __forceinline__ void bd_castle(E& emit, const Pos& b, bool kingside)
+{
+    const int base = S ? 56 : 0;
+    const u64 kf = 1ull << (base + 4), kt = 1ull << (base + (kingside ? 6 : 2));
+    const u64 rf = 1ull << (base + (kingside ? 7 : 0)), rt = 1ull << (base + (kingside ? 5 : 3));
+    Pos nb;
+    nb.bq = b.bq;
+    nb.p = b.p;
+    nb.n = b.n;
+    nb.k = (b.k ^ kf) | kt;
+    nb.rq = (b.rq ^ rf) | rt;
+    set_side(nb, 1 - S);
+    set_ep(nb, 0);
+    set_hm(nb, 0);
+    if (S == 0) {
+        nb.w = (b.w ^ (kf | rf)) | (kt | rt);
+        set_wc(nb, 0);
+    } else {
+        set_bc(nb, 0);
+        nb.w = b.w;
+    }
+    emit(nb);
+}
+// addSinglePawnMove (MGB.h:1527-1574)
+template <int S, class E> __device__ __forceinline__ void bd_step(E& emit, const Pos& b, u64 src, u64 dst, bool dbl, int from)
+{
+    Pos nb;
+    nb.bq = b.bq & ~dst;
+    nb.rq = b.rq & ~dst;
+    nb.n = b.n & ~dst;
+    nb.k = b.k;
+    nb.p = (b.p ^ src) | dst;
+    nb.w = new_white(b, S, src, dst);
+    set_side(nb, 1 - S);
+    set_ep(nb, dbl ? (from & 7) + 1 : 0);
+    set_hm(nb, 0);
+    emit(nb);
+}
+// addEnPassentMove (MGB.h:1576-1618)
+template <int S, class E> __device__ __forceinline__ void bd_ep(E& emit, const Pos& b, u64 src, u64 dst)
+{
+    const u64 victim = S ? up(dst) : down(dst);
+    Pos nb;
+    nb.bq = b.bq;
+    nb.rq = b.rq;
+    nb.n = b.n;
+    nb.k = b.k;
+    nb.p = (b.p ^ (victim | src)) | dst;
+    nb.w = S ? (b.w ^ victim) : ((b.w ^ src) | dst);
+    set_side(nb, 1 - S);
+    set_hm(nb, 0);
+    set_ep(nb, 0);
+    emit(nb);
+}
+// addPawnMoves (MGB.h:1622-1699): promotions N, B, Q, R
+template <int S, class E> __device__ __forceinline__ void bd_pawn(E& emit, const Pos& b, u64 src, u64 dst)
+{
+    if (!(dst & BACK_RANKS)) {
+        bd_step<S>(emit, b, src, dst, false, 0);
+        return;
+    }
+    Pos nb;
+    nb.k = b.k;
+    nb.w = new_white(b, S, src, dst);
+    nb.p = b.p ^ src;
+    set_side(nb, 1 - S);
+    set_ep(nb, 0);
+    set_hm(nb, 0);
+    castle_update(nb, dst, S);
+    nb.n = b.n | dst;
+    nb.bq = b.bq & ~dst;
+    nb.rq = b.rq & ~dst;
+    emit(nb);
+    nb.n = b.n & ~dst;
+    nb.bq = b.bq | dst;
+    nb.rq = b.rq & ~dst;
+    emit(nb);
+    nb.rq = b.rq | dst;
+    emit(nb);
+    nb.bq = b.bq & ~dst;
+    emit(nb);
+}
+
+template <int S, class SL, class E>
+__device__ __noinline__ void gen_boards_evasions(const Pos& b, E& emit)
+{
+    const Sides<S> c(b);
+    const u64 threat = threat_full<S, SL>(b, c);
+    for (u64 s = king_set(c.king) & ~(threat | c.mine); s; s &= s - 1) bd_king<S>(emit, b, c.king, lowbit(s));
+    const u64 att = checkers<S, SL>(b, c);
+    if (!att || several(att)) return;
+    const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
+    const u64 safe = att | between_on(king_line(c.ksq, att), lsb(att), c.ksq);
+    const u64 mine = c.mine & ~pinned;
+    u64 tgt = ep_target<S>(b);
+    const u64 victim = S ? up(tgt) : down(tgt);
+    if (victim != att) tgt = 0;
+    for (u64 pw = c.pawns & mine; pw; pw &= pw - 1) {
+        const u64 p = lowbit(pw);
+        const u64 d = push1<S>(p) & ~c.occ;
+        if (d) {
+            if (d & safe) {
+                bd_pawn<S>(emit, b, p, d);
+            } else {
+                const u64 d2 = push1<S>(d & double_rank<S>()) & safe & ~c.occ;
+                if (d2) bd_step<S>(emit, b, p, d2, true, lsb(p));
+            }
+        }
+        const u64 caps = cap_w<S>(p) | cap_e<S>(p);
+        const u64 hit = caps & c.theirs & safe;
+        if (hit) bd_pawn<S>(emit, b, p, hit);
+        const u64 epd = caps & tgt;
+        if (epd) bd_ep<S>(emit, b, p, epd);
+    }
+    for (u64 s = b.n & mine; s; s &= s - 1)
+        for (u64 m = __ldg(&g_knight[lsb(s)]) & safe; m; m &= m - 1) bd_knight<S>(emit, b, lowbit(s), lowbit(m));
+    for (u64 s = b.bq & mine; s; s &= s - 1)
+        for (u64 m = SL::bishop(lsb(s), c.occ) & safe; m; m &= m - 1) bd_slider<S>(emit, b, lowbit(s), lowbit(m));
+    for (u64 s = b.rq & mine; s; s &= s - 1)
+        for (u64 m = SL::rook(lsb(s), c.occ) & safe; m; m &= m - 1) bd_slider<S>(emit, b, lowbit(s), lowbit(m));
+}
+
+template <int S, class SL, class E>
+__device__ __forceinline__ void gen_boards(const Pos& b, E& emit)
+{
+    const Sides<S> c(b);
+    const u64 threat = threat_full<S, SL>(b, c);
+    if (threat & c.king) {
+        gen_boards_evasions<S, SL>(b, emit);
+        return;
+    }
+    const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
+    const u64 myp = c.pawns & c.mine;
+    const u64 tgt = ep_target<S>(b);
+    if (tgt) {
+        const u64 victim = S ? up(tgt) : down(tgt);
+        for (u64 s = (east1(victim) | west1(victim)) & myp; s; s &= s - 1)
+            if (ep_legal<S>(c, pinned, lowbit(s), tgt, victim)) bd_ep<S>(emit, b, lowbit(s), tgt);
+    }
+    for (u64 s = myp & pinned; s; s &= s - 1) {
+        const u64 p = lowbit(s);
+        const int from = lsb(p);
+        const u64 line = king_line(c.ksq, p);
+        const u64 d = push1<S>(p) & line & ~c.occ;
+        if (d) {
+            bd_step<S>(emit, b, p, d, false, from);
+            const u64 d2 = push1<S>(d & double_rank<S>()) & ~c.occ;
+            if (d2) bd_step<S>(emit, b, p, d2, true, from);
+        }
+        const u64 x = (cap_w<S>(p) & line) | (cap_e<S>(p) & line);
+        if (x & c.theirs) bd_pawn<S>(emit, b, p, x);
+    }
+    for (u64 s = myp & ~pinned; s; s &= s - 1) {
+        const u64 p = lowbit(s);
+        const u64 d = push1<S>(p) & ~c.occ;
+        if (d) {
+            bd_pawn<S>(emit, b, p, d);
+            const u64 d2 = push1<S>(d & double_rank<S>()) & ~c.occ;
+            if (d2) bd_step<S>(emit, b, p, d2, true, lsb(p));
+        }
+        const u64 w = cap_w<S>(p) & c.theirs;
+        if (w) bd_pawn<S>(emit, b, p, w);
+        const u64 e = cap_e<S>(p) & c.theirs;
+        if (e) bd_pawn<S>(emit, b, p, e);
+    }
+    if (can_castle_k<S>(b, c.occ, threat)) bd_castle<S>(emit, b, true);
+    if (can_castle_q<S>(b, c.occ, threat)) bd_castle<S>(emit, b, false);
+    for (u64 s = king_set(c.king) & ~(threat | c.mine); s; s &= s - 1) bd_king<S>(emit, b, c.king, lowbit(s));
+    for (u64 s = b.n & c.mine & ~pinned; s; s &= s - 1)
+        for (u64 m = __ldg(&g_knight[lsb(s)]) & ~c.mine; m; m &= m - 1) bd_knight<S>(emit, b, lowbit(s), lowbit(m));
+    const u64 my_bq = b.bq & c.mine, my_rq = b.rq & c.mine;
+    for (u64 s = my_bq & pinned; s; s &= s - 1)
+        for (u64 m = SL::bishop(lsb(s), c.occ) & ~c.mine & king_line(c.ksq, lowbit(s)); m; m &= m - 1)
+            bd_slider<S>(emit, b, lowbit(s), lowbit(m));
+    for (u64 s = my_bq & ~pinned; s; s &= s - 1)
+        for (u64 m = SL::bishop(lsb(s), c.occ) & ~c.mine; m; m &= m - 1) bd_slider<S>(emit, b, lowbit(s), lowbit(m));
+    for (u64 s = my_rq & pinned; s; s &= s - 1)
+        for (u64 m = SL::rook(lsb(s), c.occ) & ~c.mine & king_line(c.ksq, lowbit(s)); m; m &= m - 1)
+            bd_slider<S>(emit, b, lowbit(s), lowbit(m));
+    for (u64 s = my_rq & ~pinned; s; s &= s - 1)
+        for (u64 m = SL::rook(lsb(s), c.occ) & ~c.mine; m; m &= m - 1) bd_slider<S>(emit, b, lowbit(s), lowbit(m));
+}
+
+}  // namespace pg

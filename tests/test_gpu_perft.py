@@ -1,0 +1,112 @@
+"""GPU perft against the reference's counts (golden vectors), bit-exact, and
+size-independent properties at the full workload sizes."""
+import numpy as np
+import pytest
+
+from conftest import golden_json, golden_npz, words_of_hex
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("slider", ["ks", "fancy", "byte"])
+def test_reference_fens_perft(pg, slider):
+    for item in golden_json("fens.json"):
+        b = pg.board_from_fen(item["fen"])
+        for d, v in item["perft"].items():
+            assert pg.perft(b, int(d), slider=slider) == v, (item["name"], d, slider)
+
+
+@pytest.mark.parametrize("block", [128, 256, 512])
+def test_block_sizes(pg, block):
+    item = golden_json("fens.json")[1]
+    b = pg.board_from_fen(item["fen"])
+    assert pg.perft(b, 5, block_size=block) == item["perft"]["5"]
+
+
+def test_divide_matches_reference(pg):
+    for item in golden_json("fens.json"):
+        b = pg.board_from_fen(item["fen"])
+        assert [[m, c] for m, c in pg.perft_divide(b, 3)] == item["divide3"], item["name"]
+
+
+def test_depth_edges(pg):
+    b = pg.board_from_fen("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1")
+    assert pg.perft(b, 0) == 1
+    assert pg.perft(b, 1) == 20
+    assert pg.perft(b, 2) == 400
+    mate = pg.board_from_fen("rnb1kbnr/pppp1ppp/8/4p3/6Pq/5P2/PPPPP2P/RNBQKBNR w KQkq - 1 3")
+    assert pg.count_moves(mate) == 0
+    assert pg.perft(mate, 1) == 0 and pg.perft(mate, 3) == 0
+    stale = pg.board_from_fen("7k/5Q2/6K1/8/8/8/8/8 b - - 0 1")
+    assert pg.count_moves(stale) == 0 and pg.perft(stale, 4) == 0
+    out = pg.perft_batch(np.zeros(0, dtype=pg.BOARD_DTYPE), [])
+    assert len(out) == 0
+
+
+def test_config1_batch_and_divide(pg):
+    g = golden_json("config1.json")
+    boards = np.array([words_of_hex(p["board"]) for p in g["positions"]], dtype=np.uint64)
+    boards = boards.view(pg.BOARD_DTYPE).reshape(-1)
+    depths = [p["depth"] for p in g["positions"]]
+    out = pg.perft_batch(boards, depths, slider="ks")
+    assert [int(x) for x in out] == [p["total"] for p in g["positions"]]
+    for p in g["positions"][:8]:
+        got = pg.perft_divide(pg.HexaBitBoardPosition(*words_of_hex(p["board"])), p["depth"])
+        assert [[m, c] for m, c in got] == p["divide"]
+
+
+def test_config2_deep_single_position(pg):
+    g = golden_json("config2.json")
+    b = pg.HexaBitBoardPosition(*words_of_hex(g["board"]))
+    assert pg.count_moves(b) >= 35
+    assert pg.perft(b, 5) == g["perft5"]
+    assert pg.perft(b, 6) == g["perft6"]
+    assert [[m, c] for m, c in pg.perft_divide(b, 6)] == g["divide6"]
+
+
+@pytest.mark.slow
+def test_config2_depth7(pg):
+    g = golden_json("config2.json")
+    b = pg.HexaBitBoardPosition(*words_of_hex(g["board"]))
+    assert pg.perft(b, 7) == g["perft7"]
+
+
+def test_config3_batched_uneven(pg):
+    g = golden_npz("config3.npz")
+    boards = g["boards"].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    out = pg.perft_batch(boards, g["depths"])
+    assert np.array_equal(out, g["totals"])
+
+
+def test_config3_playouts_regenerate_on_gpu(pg):
+    g = golden_npz("config3.npz")
+    boards, depths = pg.random_playouts(3, 4096, 0, 60, 1, 3, 6, with_depths=True)
+    assert np.array_equal(boards.view(np.uint64).reshape(-1, 6), g["boards"])
+    assert np.array_equal(depths, g["depths"])
+
+
+def test_chunked_levels_small_budget(pg):
+    """A small HBM budget forces every expansion into many chunks."""
+    item = golden_json("fens.json")[1]
+    pg.shutdown()
+    pg.init(hbm_budget_bytes=64 << 20)
+    try:
+        b = pg.board_from_fen(item["fen"])
+        assert pg.perft(b, 5) == item["perft"]["5"]
+        g = golden_npz("config4_d5.npz")
+        boards = g["boards"][:64].copy().view(pg.BOARD_DTYPE).reshape(-1)
+        assert np.array_equal(pg.perft_batch(boards, [5] * 64), g["totals"][:64])
+    finally:
+        pg.shutdown()
+        pg.init()
+
+
+def test_batch_equals_sum_of_singles(pg):
+    """Each result alone equals its result inside a mixed batch."""
+    g = golden_npz("config3.npz")
+    idx = np.arange(0, 4096, 97)
+    boards = g["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    depths = np.minimum(g["depths"][idx], 5)
+    mixed = pg.perft_batch(boards, depths)
+    alone = [pg.perft(pg.board_of(boards[i]), int(depths[i])) for i in range(len(idx))]
+    assert [int(x) for x in mixed] == alone
