@@ -95,6 +95,10 @@ int pg_shutdown(void);
 const char *pg_last_error(void);
 /* Utils::readFENString + board088ToHexBB (util.cpp:189-280, util.cpp:92-140). */
 int pg_board_from_fen(const char *fen, pg_board *out);
+/* The CUDA stream (cudaStream_t) every engine launch is issued on, so a
+ * caller can order its own work or record CUDA events around engine calls.
+ * No counterpart in the reference, which launches on the default stream. */
+int pg_get_stream(void **stream);
 
 /* ---- operator surface (GPU kernels, one position per call or a batch) ---- */
 /* countMoves<c> (MoveGeneratorBitboard.h:3008-3295). */

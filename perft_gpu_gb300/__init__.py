@@ -125,6 +125,7 @@ _SIGNATURES = {
     "pg_shutdown": [],
     "pg_last_error": [],
     "pg_board_from_fen": [ctypes.c_char_p, _BP],
+    "pg_get_stream": [ctypes.POINTER(ctypes.c_void_p)],
     "pg_count_moves": [_BP, _U32P],
     "pg_count_moves_batch": [_BP, ctypes.c_uint32, _U32P],
     "pg_generate_moves": [_BP, _U16P, _U32P],
@@ -197,6 +198,13 @@ def init(device: int = 0, hbm_budget_bytes: int = 0, slider: int | str = 0, verb
 
 def shutdown():
     _check(load_library().pg_shutdown())
+
+
+def get_stream() -> int:
+    """The engine's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+    s = ctypes.c_void_p()
+    _check(load_library().pg_get_stream(ctypes.byref(s)))
+    return s.value or 0
 
 
 def board_from_fen(fen: str) -> HexaBitBoardPosition:

@@ -365,6 +365,17 @@ extern "C" {
 
 const char* pg_last_error(void) { return t_error.c_str(); }
 
+int pg_get_stream(void** stream)
+{
+    if (!stream) {
+        set_error("null argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    PG_TRY(check_ready());
+    *stream = (void*)engine().stream;
+    return PG_OK;
+}
+
 int pg_init(const pg_config* cfg)
 {
     Engine& E = engine();

@@ -231,9 +231,15 @@ template <class SL, int T, int QCAP> struct BlockSmem {
     static constexpr int bytes = tables + boards + queue + T * 4 + T;
 };
 
+// register cap: at least PG_LEAF_MIN_WARPS resident warps per SM
+#ifndef PG_LEAF_MIN_WARPS
+#define PG_LEAF_MIN_WARPS 16
+#endif
+template <int T> constexpr int min_blocks() { return (PG_LEAF_MIN_WARPS * 32 + T - 1) / T; }
+
 // the last plies of every node with remaining depth <= 2, inside one CTA
 template <int S, class SL, int T, int QCAP>
-__global__ void __launch_bounds__(T) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket)
+__global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket)
 {
     extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     stage_tables<SL>();
@@ -289,7 +295,7 @@ __global__ void __launch_bounds__(T) k_leaf(LevelView lv, u32 start, u32 n, u64*
 // children of the nodes [a, b) of a level into the next level; offs is the
 // exclusive scan of the children counts, child slots start at offs[a]
 template <int S, class SL, int T, int QCAP>
-__global__ void __launch_bounds__(T) k_expand(LevelView in, u32 start, u32 a, u32 b, const u64* __restrict__ offs,
+__global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32 start, u32 a, u32 b, const u64* __restrict__ offs,
                                               LevelView out, u32* ticket)
 {
     extern __shared__ __align__(16) unsigned char pg_dyn_smem[];

@@ -292,10 +292,163 @@ __device__ __noinline__ u32 count_pawn_specials(const Pos& b, u64 pinned)
     return n;
 }
 
+// One line through the king (two opposite directions that share a step),
+// scanned with the propagator chains of those directions: the enemy sliders'
+// fills give the attacked squares, the king's own fills give its first
+// blockers, and their intersection gives pins and checks without a branch.
+struct LineScan {
+    u64 threat;    // enemy slider attacks along the line (king on the board)
+    u64 pinned;    // own pieces pinned along this line
+    u64 checkers;  // enemy sliders giving check along this line
+    u64 chk_ray;   // squares from the king to each such checker, checker included
+    u64 xray;      // the square beyond the king, away from a checker
+};
+
+template <int SH>
+__device__ __forceinline__ LineScan scan_line(const Pro<SH, true>& up_, const Pro<SH, false>& dn, u64 sliders,
+                                              u64 king, u64 mine)
+{
+    LineScan o;
+    const u64 a_up = up_.attacks(sliders), a_dn = dn.attacks(sliders);
+    const u64 k_up = up_.attacks(king), k_dn = dn.attacks(king);
+    o.threat = a_up | a_dn;
+    o.pinned = ((k_up & a_dn) | (k_dn & a_up)) & mine;
+    const u64 c_up = k_up & sliders, c_dn = k_dn & sliders;
+    o.checkers = c_up | c_dn;
+    o.chk_ray = (c_up ? k_up : 0ull) | (c_dn ? k_dn : 0ull);
+    o.xray = (c_up ? (shf<SH, false>(king) & DirMask<SH, false>::keep) : 0ull) |
+             (c_dn ? (shf<SH, true>(king) & DirMask<SH, true>::keep) : 0ull);
+    return o;
+}
+
+// en passant for the branch-free count (rare: the file is set only when a
+// capture is possible).  Outside check: MGB.h:3058-3093; in check only when
+// the pushed pawn is the single checker (MGB.h:2903-2906, 2948-2953).
+template <int S>
+__device__ __noinline__ u32 count_ep_ks(const Pos& b, u64 pinned, u64 checkers)
+{
+    const Sides<S> c(b);
+    const u64 tgt = ep_target<S>(b);
+    const u64 victim = S ? up(tgt) : down(tgt);
+    const u64 myp = c.pawns & c.mine;
+    if (checkers) {
+        if (victim != checkers) return 0;
+        const u64 fp = myp & ~pinned;
+        return popc(cap_w<S>(fp) & tgt) + popc(cap_e<S>(fp) & tgt);
+    }
+    u32 n = 0;
+    for (u64 s = (east1(victim) | west1(victim)) & myp; s; s &= s - 1)
+        n += ep_legal<S>(c, pinned, lowbit(s), tgt, victim) ? 1 : 0;
+    return n;
+}
+
+// countMoves / countMovesOutOfCheck (MGB.h:3008-3295, 2825-3002) as one
+// instruction stream for the Kogge-Stone policy.  Check handling is a target
+// mask: ~own outside check, the check ray (between squares + checker) in
+// single check, nothing in double check; pinned pieces move along their pin
+// line outside check and not at all in check.  The counts are the
+// reference's in every case (proved per term in the comments of the
+// reference-shaped paths above and checked bit-exact by the tests).
+template <int S>
+__device__ __forceinline__ u32 count_moves_ks(const Pos& b)
+{
+    const u64 pawns = b.p & INNER;
+    const u64 occ = b.k | pawns | b.n | b.bq | b.rq;
+    const u64 black = occ & ~b.w;
+    const u64 mine = S ? black : b.w, theirs = S ? b.w : black;
+    const u64 king = b.k & mine;
+    const u64 empty = ~occ;
+    const u64 trq = b.rq & theirs, tbq = b.bq & theirs;
+    const u64 tp = pawns & theirs, tn = b.n & theirs;
+
+    // pass 1: enemy fills and king fills per line (pins, checks, x-rays)
+    LineScan lf, lr, ld, la;
+    {
+        const Pro<8, true> a(empty);
+        const Pro<8, false> c(empty);
+        lf = scan_line(a, c, trq, king, mine);
+    }
+    {
+        const Pro<1, true> a(empty);
+        const Pro<1, false> c(empty);
+        lr = scan_line(a, c, trq, king, mine);
+    }
+    {
+        const Pro<9, true> a(empty);
+        const Pro<9, false> c(empty);
+        ld = scan_line(a, c, tbq, king, mine);
+    }
+    {
+        const Pro<7, true> a(empty);
+        const Pro<7, false> c(empty);
+        la = scan_line(a, c, tbq, king, mine);
+    }
+
+    const u64 pinned = lf.pinned | lr.pinned | ld.pinned | la.pinned;
+    const u64 nchk = knight_set(king) & tn;
+    const u64 pchk = pawn_attackers_of<S>(king) & tp;
+    const u64 checkers = lf.checkers | lr.checkers | ld.checkers | la.checkers | nchk | pchk;
+    const u64 threat = lf.threat | lr.threat | ld.threat | la.threat | pawn_attacks<1 - S>(tp) | knight_set(tn) |
+                       king_set(b.k & theirs);
+    const u64 xray = lf.xray | lr.xray | ld.xray | la.xray;
+    const u64 safe = lf.chk_ray | lr.chk_ray | ld.chk_ray | la.chk_ray | nchk | pchk;
+    const bool in_check = checkers != 0;
+    const u64 chk_all = in_check ? ~0ull : 0ull;
+    const u64 tgt = several(checkers) ? 0ull : (in_check ? safe : ~mine);
+
+    u32 n = popc(king_set(king) & ~(threat | mine | xray));
+
+    // pass 2: own slider moves.  The propagator chains are rebuilt from an
+    // opaque copy of `empty` so the compiler does not keep pass 1's chains
+    // alive (a few more ALU operations for far fewer live registers).
+    u64 empty2 = empty;
+    asm volatile("" : "+l"(empty2));
+    const u64 my_rq = b.rq & mine, my_bq = b.bq & mine;
+    const u64 pin_chk = pinned & chk_all;
+    {
+        const u64 ns = my_rq & ~((pinned ^ lf.pinned) | pin_chk);
+        n += popc(Pro<8, true>(empty2).attacks(ns) & tgt) + popc(Pro<8, false>(empty2).attacks(ns) & tgt);
+    }
+    {
+        const u64 ew = my_rq & ~((pinned ^ lr.pinned) | pin_chk);
+        n += popc(Pro<1, true>(empty2).attacks(ew) & tgt) + popc(Pro<1, false>(empty2).attacks(ew) & tgt);
+    }
+    {
+        const u64 dg = my_bq & ~((pinned ^ ld.pinned) | pin_chk);
+        n += popc(Pro<9, true>(empty2).attacks(dg) & tgt) + popc(Pro<9, false>(empty2).attacks(dg) & tgt);
+    }
+    {
+        const u64 ad = my_bq & ~((pinned ^ la.pinned) | pin_chk);
+        n += popc(Pro<7, true>(empty2).attacks(ad) & tgt) + popc(Pro<7, false>(empty2).attacks(ad) & tgt);
+    }
+
+    for (u64 s = b.n & mine & ~pinned; s; s &= s - 1) n += popc(__ldg(&g_knight[lsb(s)]) & tgt);
+
+    // pawns: pushes by free pawns and file-pinned pawns, captures by free
+    // pawns and pawns pinned on that capture's diagonal; pinned pawns only
+    // outside check.  In check a double push counts only when the single
+    // push does not already answer the check.
+    const u64 myp = pawns & mine;
+    const u64 fp = myp & ~pinned;
+    const u64 pin_ok = ~chk_all;
+    const u64 d1 = push1<S>(fp | (myp & lf.pinned & pin_ok)) & empty;
+    const u64 s1 = d1 & tgt;
+    n += popc(s1) + 3 * popc(s1 & BACK_RANKS);
+    n += popc(push1<S>(d1 & double_rank<S>() & ~safe) & empty & tgt);
+    const u64 cw = cap_w<S>(fp | (myp & (S ? ld.pinned : la.pinned) & pin_ok)) & theirs & tgt;
+    const u64 ce = cap_e<S>(fp | (myp & (S ? la.pinned : ld.pinned) & pin_ok)) & theirs & tgt;
+    n += popc(cw) + popc(ce) + 3 * (popc(cw & BACK_RANKS) + popc(ce & BACK_RANKS));
+
+    if (!in_check) n += can_castle_k<S>(b, occ, threat) + can_castle_q<S>(b, occ, threat);
+    if (b.p & 0xF0ull) n += count_ep_ks<S>(b, pinned, checkers);
+    return n;
+}
+
 // countMoves (MGB.h:3008-3295)
 template <int S, class SL>
 __device__ __forceinline__ u32 count_moves(const Pos& b)
 {
+    if constexpr (SL::kId == 0) return count_moves_ks<S>(b);
     const Sides<S> c(b);
     const u64 empty = ~c.occ;
     const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
