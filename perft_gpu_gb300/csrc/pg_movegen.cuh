@@ -32,8 +32,8 @@ namespace pg {
 // Every translation unit that includes this header owns one copy of the
 // tables (non-relocatable device code gives __device__ variables internal
 // linkage) and uploads it through its own upload function at pg_init.
-static __device__ MagicSq g_magic_rook[64];
-static __device__ MagicSq g_magic_bishop[64];
+static __device__ __align__(16) MagicSq g_magic_rook[64];
+static __device__ __align__(16) MagicSq g_magic_bishop[64];
 static __device__ u64 g_magic_attacks[MAGIC_TABLE_ENTRIES];
 static __device__ __align__(16) unsigned char g_magic_bytes[MAGIC_TABLE_ENTRIES];
 static __device__ u64 g_magic_unique[UNIQUE_TOTAL];
@@ -53,9 +53,11 @@ struct SlFancy {
     static constexpr bool kSetwise = false;
     __device__ __forceinline__ static u64 look(const MagicSq* t, int sq, u64 occ)
     {
-        const u64 mask = __ldg(&t[sq].mask), magic = __ldg(&t[sq].magic);
-        const u32 off = __ldg(&t[sq].offset), sh = __ldg(&t[sq].shift);
-        return __ldg(&g_magic_attacks[off + (u32)(((occ & mask) * magic) >> sh)]);
+        // one 32-byte entry as two 16-byte loads: (mask, magic), (offset, shift, ...)
+        const uint4* e = reinterpret_cast<const uint4*>(t + sq);
+        const uint4 a = __ldg(e), c = __ldg(e + 1);
+        const u64 mask = ((u64)a.y << 32) | a.x, magic = ((u64)a.w << 32) | a.z;
+        return __ldg(&g_magic_attacks[c.x + (u32)(((occ & mask) * magic) >> c.y)]);
     }
     __device__ __forceinline__ static u64 bishop(int sq, u64 occ) { return look(g_magic_bishop, sq, occ); }
     __device__ __forceinline__ static u64 rook(int sq, u64 occ) { return look(g_magic_rook, sq, occ); }
@@ -231,67 +233,6 @@ template <int S, class SL> __device__ __forceinline__ u64 checkers(const Pos& b,
 // countMoves
 // ---------------------------------------------------------------------------
 
-// countMovesOutOfCheck (MGB.h:2825-3002); counted set-wise where the
-// per-piece sums are provably equal.
-template <int S, class SL>
-__device__ __noinline__ u32 count_evasions(const Pos& b)
-{
-    const Sides<S> c(b);
-    const u64 threat = threat_full<S, SL>(b, c);
-    u32 n = popc(king_set(c.king) & ~(threat | c.mine));
-    const u64 att = checkers<S, SL>(b, c);
-    if (!att || several(att)) return n;
-    const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
-    const int asq = lsb(att);
-    const u64 safe = att | between_on(king_line(c.ksq, att), asq, c.ksq);
-    const u64 mine = c.mine & ~pinned;
-    const u64 empty = ~c.occ;
-    const u64 P = c.pawns & mine;
-    // pushes: a safe single push (4 if promotion); otherwise a safe double push
-    const u64 d1 = push1<S>(P) & empty;
-    n += popc(d1 & safe) + 3 * popc(d1 & safe & BACK_RANKS);
-    n += popc(push1<S>(d1 & ~safe & double_rank<S>()) & safe & empty);
-    // captures of the checker
-    const u64 hitw = cap_w<S>(P) & c.theirs & safe, hite = cap_e<S>(P) & c.theirs & safe;
-    n += (popc(hitw) + popc(hite)) * ((att & BACK_RANKS) ? 4 : 1);
-    // en passant only when the double-pushed pawn is the checker
-    u64 tgt = ep_target<S>(b);
-    const u64 victim = S ? up(tgt) : down(tgt);
-    if (victim != att) tgt = 0;
-    n += popc(cap_w<S>(P) & tgt) + popc(cap_e<S>(P) & tgt);
-    for (u64 s = b.n & mine; s; s &= s - 1) n += popc(knight_set(lowbit(s)) & safe);
-    for (u64 s = b.bq & mine; s; s &= s - 1) n += popc(SL::bishop(lsb(s), c.occ) & safe);
-    for (u64 s = b.rq & mine; s; s &= s - 1) n += popc(SL::rook(lsb(s), c.occ) & safe);
-    return n;
-}
-
-// pinned pawns and en passant outside check (rare; kept out of line)
-template <int S>
-__device__ __noinline__ u32 count_pawn_specials(const Pos& b, u64 pinned)
-{
-    const Sides<S> c(b);
-    const u64 myp = c.pawns & c.mine;
-    u32 n = 0;
-    const u64 tgt = ep_target<S>(b);
-    if (tgt) {
-        const u64 victim = S ? up(tgt) : down(tgt);
-        for (u64 s = (east1(victim) | west1(victim)) & myp; s; s &= s - 1)
-            n += ep_legal<S>(c, pinned, lowbit(s), tgt, victim) ? 1 : 0;
-    }
-    for (u64 s = myp & pinned; s; s &= s - 1) {
-        const u64 p = lowbit(s);
-        const u64 line = king_line(c.ksq, p);
-        const u64 d = push1<S>(p) & line & ~c.occ;
-        if (d) {
-            n++;
-            if (push1<S>(d & double_rank<S>()) & ~c.occ) n++;
-        }
-        const u64 x = (cap_w<S>(p) & line) | (cap_e<S>(p) & line);
-        if (x & c.theirs) n += (x & BACK_RANKS) ? 4 : 1;
-    }
-    return n;
-}
-
 // One line through the king (two opposite directions that share a step),
 // scanned with the propagator chains of those directions: the enemy sliders'
 // fills give the attacked squares, the king's own fills give its first
@@ -444,99 +385,96 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     return n;
 }
 
+// countMoves / countMovesOutOfCheck (MGB.h:3008-3295, 2825-3002) for the
+// table policies, in the same mask form as count_moves_ks: one lookup per
+// slider for the enemy attacks and for the own moves (the 64-bit multiply
+// runs on the FMA pipe, the table read on the load pipe), two lookups from
+// the king square for checks, and two x-ray lookups through the king's own
+// first blockers for pins.  A pinner's rays meet the king's rays only on the
+// pin line (the pinner's other line is parallel to the king's other line of
+// the same kind), so `own first blockers & pinner attacks` is exactly the
+// pinned piece.
+template <int S, class SL>
+__device__ __forceinline__ u32 count_moves_mg(const Pos& b)
+{
+    const u64 pawns = b.p & INNER;
+    const u64 occ = b.k | pawns | b.n | b.bq | b.rq;
+    const u64 black = occ & ~b.w;
+    const u64 mine = S ? black : b.w, theirs = S ? b.w : black;
+    const u64 king = b.k & mine;
+    const int ksq = lsb(king) & 63;
+    const u64 empty = ~occ;
+    const u64 trq = b.rq & theirs, tbq = b.bq & theirs;
+    const u64 tp = pawns & theirs, tn = b.n & theirs;
+
+    u64 threat = pawn_attacks<1 - S>(tp) | knight_set(tn) | king_set(b.k & theirs);
+    for (u64 s = trq; s; s &= s - 1) threat |= SL::rook(lsb(s), occ);
+    for (u64 s = tbq; s; s &= s - 1) threat |= SL::bishop(lsb(s), occ);
+
+    const u64 ra = SL::rook(ksq, occ), ba = SL::bishop(ksq, occ);
+    const u64 nchk = knight_set(king) & tn;
+    const u64 pchk = pawn_attackers_of<S>(king) & tp;
+    const u64 schk = (ra & trq) | (ba & tbq);
+    const u64 checkers = schk | nchk | pchk;
+    u64 safe = nchk | pchk;
+    u64 behind = 0;  // squares a checking slider attacks through the king
+    for (u64 s = schk; s; s &= s - 1) {
+        const int c = lsb(s);
+        const u64 cb = 1ull << c;
+        const bool orth = (ra & cb) != 0;
+        safe |= ((orth ? ra : ba) & (orth ? SL::rook(c, occ) : SL::bishop(c, occ))) | cb;
+        behind |= orth ? SL::rook(c, occ ^ king) : SL::bishop(c, occ ^ king);
+    }
+    const u64 rb = ra & mine, bb = ba & mine;
+    const u64 pin_r = SL::rook(ksq, occ ^ rb) & ~ra & trq;
+    const u64 pin_b = SL::bishop(ksq, occ ^ bb) & ~ba & tbq;
+    u64 pinned = 0;
+    for (u64 s = pin_r; s; s &= s - 1) pinned |= rb & SL::rook(lsb(s), occ);
+    for (u64 s = pin_b; s; s &= s - 1) pinned |= bb & SL::bishop(lsb(s), occ);
+
+    const bool in_check = checkers != 0;
+    const u64 chk_all = in_check ? ~0ull : 0ull;
+    const u64 tgt = several(checkers) ? 0ull : (in_check ? safe : ~mine);
+    u32 n = popc(king_set(king) & ~(threat | behind | mine));
+
+    const u64 lf = file_of(ksq), lr = rank_of(ksq), ld = diag_of(ksq), la = anti_of(ksq);
+    const u64 stay = pinned & chk_all;  // in check a pinned piece never moves
+    for (u64 s = b.rq & mine & ~stay; s; s &= s - 1) {
+        const int sq = lsb(s);
+        const u64 bit = 1ull << sq;
+        const u64 line = (pinned & bit) ? ((lf & bit) ? lf : (lr & bit) ? lr : (ld & bit) ? ld : la) : ~0ull;
+        n += popc(SL::rook(sq, occ) & tgt & line);
+    }
+    for (u64 s = b.bq & mine & ~stay; s; s &= s - 1) {
+        const int sq = lsb(s);
+        const u64 bit = 1ull << sq;
+        const u64 line = (pinned & bit) ? ((lf & bit) ? lf : (lr & bit) ? lr : (ld & bit) ? ld : la) : ~0ull;
+        n += popc(SL::bishop(sq, occ) & tgt & line);
+    }
+    for (u64 s = b.n & mine & ~pinned; s; s &= s - 1) n += popc(__ldg(&g_knight[lsb(s)]) & tgt);
+
+    const u64 myp = pawns & mine;
+    const u64 fp = myp & ~pinned;
+    const u64 pin_ok = ~chk_all;
+    const u64 d1 = push1<S>(fp | (myp & pinned & lf & pin_ok)) & empty;
+    const u64 s1 = d1 & tgt;
+    n += popc(s1) + 3 * popc(s1 & BACK_RANKS);
+    n += popc(push1<S>(d1 & double_rank<S>() & ~safe) & empty & tgt);
+    const u64 cw = cap_w<S>(fp | (myp & pinned & (S ? ld : la) & pin_ok)) & theirs & tgt;
+    const u64 ce = cap_e<S>(fp | (myp & pinned & (S ? la : ld) & pin_ok)) & theirs & tgt;
+    n += popc(cw) + popc(ce) + 3 * (popc(cw & BACK_RANKS) + popc(ce & BACK_RANKS));
+
+    if (!in_check) n += can_castle_k<S>(b, occ, threat) + can_castle_q<S>(b, occ, threat);
+    if (b.p & 0xF0ull) n += count_ep_ks<S>(b, pinned, checkers);
+    return n;
+}
+
 // countMoves (MGB.h:3008-3295)
 template <int S, class SL>
 __device__ __forceinline__ u32 count_moves(const Pos& b)
 {
     if constexpr (SL::kId == 0) return count_moves_ks<S>(b);
-    const Sides<S> c(b);
-    const u64 empty = ~c.occ;
-    const u64 pinned = find_pinned(c.ksq, c.tbq, c.trq, c.occ);
-    const u64 my_bq = b.bq & c.mine, my_rq = b.rq & c.mine;
-
-    // enemy attacks.  Outside check no enemy ray reaches the king, so the
-    // rays through the king's square need not be extended; in check the
-    // evasion path recomputes them with the king removed.
-    u64 threat = pawn_attacks<1 - S>(c.pawns & c.theirs) | knight_set(b.n & c.theirs) | king_set(b.k & c.theirs);
-    u32 n = 0;
-    if constexpr (SL::kSetwise) {
-        // own sliders split by the one line they may still move along
-        const u64 pl = pinned & c.mine;
-        const u64 ns = my_rq & ~(pl & ~file_of(c.ksq));
-        const u64 ew = my_rq & ~(pl & ~rank_of(c.ksq));
-        const u64 dg = my_bq & ~(pl & ~diag_of(c.ksq));
-        const u64 ad = my_bq & ~(pl & ~anti_of(c.ksq));
-        const u64 tgt_mask = ~c.mine;
-        {
-            const Pro<8, true> pr(empty);
-            threat |= pr.attacks(c.trq);
-            n += popc(pr.attacks(ns) & tgt_mask);
-        }
-        {
-            const Pro<8, false> pr(empty);
-            threat |= pr.attacks(c.trq);
-            n += popc(pr.attacks(ns) & tgt_mask);
-        }
-        {
-            const Pro<1, true> pr(empty);
-            threat |= pr.attacks(c.trq);
-            n += popc(pr.attacks(ew) & tgt_mask);
-        }
-        {
-            const Pro<1, false> pr(empty);
-            threat |= pr.attacks(c.trq);
-            n += popc(pr.attacks(ew) & tgt_mask);
-        }
-        {
-            const Pro<9, true> pr(empty);
-            threat |= pr.attacks(c.tbq);
-            n += popc(pr.attacks(dg) & tgt_mask);
-        }
-        {
-            const Pro<9, false> pr(empty);
-            threat |= pr.attacks(c.tbq);
-            n += popc(pr.attacks(dg) & tgt_mask);
-        }
-        {
-            const Pro<7, true> pr(empty);
-            threat |= pr.attacks(c.tbq);
-            n += popc(pr.attacks(ad) & tgt_mask);
-        }
-        {
-            const Pro<7, false> pr(empty);
-            threat |= pr.attacks(c.tbq);
-            n += popc(pr.attacks(ad) & tgt_mask);
-        }
-        if (threat & c.king) return count_evasions<S, SL>(b);
-    } else {
-        threat |= bishops_of<SL>(c.tbq, c.occ) | rooks_of<SL>(c.trq, c.occ);
-        if (threat & c.king) return count_evasions<S, SL>(b);
-        for (u64 s = my_bq; s; s &= s - 1) {
-            const int sq = lsb(s);
-            u64 m = SL::bishop(sq, c.occ) & ~c.mine;
-            if (pinned & (1ull << sq)) m &= king_line(c.ksq, 1ull << sq);
-            n += popc(m);
-        }
-        for (u64 s = my_rq; s; s &= s - 1) {
-            const int sq = lsb(s);
-            u64 m = SL::rook(sq, c.occ) & ~c.mine;
-            if (pinned & (1ull << sq)) m &= king_line(c.ksq, 1ull << sq);
-            n += popc(m);
-        }
-    }
-
-    const u64 myp = c.pawns & c.mine;
-    if ((myp & pinned) | (b.p & 0xF0ull)) n += count_pawn_specials<S>(b, pinned);
-    const u64 fp = myp & ~pinned;
-    const u64 d1 = push1<S>(fp) & empty;
-    n += popc(d1) + 3 * popc(d1 & BACK_RANKS);
-    n += popc(push1<S>(d1 & double_rank<S>()) & empty);
-    const u64 cw = cap_w<S>(fp) & c.theirs, ce = cap_e<S>(fp) & c.theirs;
-    n += popc(cw) + popc(ce) + 3 * (popc(cw & BACK_RANKS) + popc(ce & BACK_RANKS));
-    n += can_castle_k<S>(b, c.occ, threat) + can_castle_q<S>(b, c.occ, threat);
-    n += popc(king_set(c.king) & ~(threat | c.mine));
-    for (u64 s = b.n & c.mine & ~pinned; s; s &= s - 1) n += popc(__ldg(&g_knight[lsb(s)]) & ~c.mine);
-    return n;
+    else return count_moves_mg<S, SL>(b);
 }
 
 // ---------------------------------------------------------------------------
