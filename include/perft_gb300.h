@@ -129,6 +129,24 @@ int pg_perft_batch(const pg_board *pos, const uint8_t *depths, uint32_t n, uint6
 int pg_perft_batch_device(const pg_board *d_pos, const uint8_t *d_depths, uint32_t n,
                           uint64_t *d_out, const pg_opts *opts);
 
+/* Batched perft for callers that cannot allocate device memory: a process
+ * whose memory pool already owns the whole GPU, a framework allocator that
+ * forbids side allocations, or code running where allocation is not
+ * allowed.  No counterpart in the reference.  d_pos / d_depths / d_out are
+ * device pointers owned by the caller; all working memory is one file-scope
+ * device array of 60 MiB that every GPU loading this library keeps until
+ * the process exits, so the call makes no cudaMalloc, cudaFree or other
+ * allocating call.  Limits: n <= 65536 positions, depths 0..3, and at most
+ * 1,048,576 children of the depth-3 positions; larger requests return
+ * PG_ERR_CAPACITY before any work.  The first call on a device looks up the
+ * array's device address and uploads one small table; make that first call
+ * before any stream capture.  stream may be NULL (the default stream); the
+ * call returns when d_out is written.  Every call reuses the same array, so
+ * calls that overlap on the GPU (other threads, other streams) race.  Does
+ * not need pg_init. */
+int pg_perft_batch_noalloc(const pg_board *d_pos, const uint8_t *d_depths, uint32_t n,
+                           uint64_t *d_out, void *stream);
+
 /* ---- inputs ---- */
 /* Seeded random legal playouts from the initial position, generated on the
  * GPU.  Position i is the first accepted attempt a = 0, 1, ... of:
