@@ -211,6 +211,75 @@ def run_reference(args):
     return 0
 
 
+SERVE_SEED = 5
+
+
+def serve_requests(pg, n, seed=SERVE_SEED):
+    """Request stream: playout positions (0-60 plies) and depths drawn from a
+    lognormal (median 4, sigma 0.25) rounded and clipped to 3..8."""
+    boards = pg.random_playouts(seed, n, 0, 60, 1)
+    rng = np.random.default_rng(seed)
+    depths = np.clip(np.rint(np.exp(rng.normal(np.log(4.0), 0.25, n))), 3, 8).astype(np.uint8)
+    return boards, depths, rng
+
+
+def pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if len(xs) else None
+
+
+def serve_leg(pg, rates, seconds, plain_rate):
+    """Poisson arrivals at each rate for `seconds`; the server admits, batches
+    and completes them; latency is measured by the server from submit to
+    completion.  The plain path serves the same stream one pg_perft call per
+    request, in arrival order."""
+    import threading
+    max_n = int(max(rates + [plain_rate]) * seconds * 1.5) + 64
+    boards, depths, rng = serve_requests(pg, max_n)
+    out = {"requests": "seeded playout positions (0-60 plies), depth lognormal(median 4, sigma 0.25) "
+                       "clipped to 3..8; Poisson arrivals", "rates": []}
+    check_n = 0
+    for rate in rates:
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, max_n))
+        n = int(np.searchsorted(arrivals, seconds))
+        srv = pg.Server(hbm_budget_bytes=8 << 30)
+        ids = []
+        t0 = time.perf_counter()
+        for i in range(n):
+            dt = t0 + arrivals[i] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(pg.board_of(boards[i]), int(depths[i])))
+        res = [srv.wait(r, timeout=900) for r in ids]
+        wall = time.perf_counter() - t0
+        srv.stop()
+        lat = [l for _, l in res]
+        leaves = sum(int(r) for r, _ in res)
+        # every served count equals the batch engine's count for that request
+        ref = pg.perft_batch(boards[:n], depths[:n])
+        assert [int(r) for r, _ in res] == [int(x) for x in ref], "served counts differ"
+        check_n += n
+        out["rates"].append({"rate_req_s": rate, "requests": n, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+                             "max_ms": max(lat) if lat else None, "leaves_per_s": leaves / wall,
+                             "completed_per_s": n / wall})
+    # plain: one engine call per request, FIFO, same kind of stream
+    arrivals = np.cumsum(rng.exponential(1.0 / plain_rate, max_n))
+    n = int(np.searchsorted(arrivals, seconds))
+    lat = []
+    leaves = 0
+    t0 = time.perf_counter()
+    for i in range(n):
+        dt = t0 + arrivals[i] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        leaves += pg.perft(pg.board_of(boards[i]), int(depths[i]))
+        lat.append(1e3 * (time.perf_counter() - (t0 + arrivals[i])))
+    wall = time.perf_counter() - t0
+    out["plain"] = {"rate_req_s": plain_rate, "requests": n, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+                    "leaves_per_s": leaves / wall, "path": "one pg_perft call per request, arrival order"}
+    out["verified_requests"] = check_n
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local, dist = dist_setup()
@@ -325,6 +394,11 @@ def run_ours(args):
             # DRAM bytes per leaf-parent node from the ncu capture, scaled to a launch
             traffic = tj["dram_bytes_per_leaf_parent"] * leaf_nodes / max(leaf_launches, 1)
 
+        served = None
+        if not args.no_serve:
+            rates = [float(x) for x in args.serve_rates.split(",")]
+            served = serve_leg(pg, rates, args.serve_seconds, rates[len(rates) // 2])
+
         cpu = None
         if not args.no_cpu:
             idx = np.arange(0, n, args.cpu_stride)
@@ -363,6 +437,7 @@ def run_ours(args):
                             "ms_per_launch": per_launch_ms,
                             "share_of_timed": leaf_ms / (elapsed * 1e3)},
             "cpu_baseline": cpu,
+            "served": served,
             "clocks": clk,
         }
     barrier(dist)
@@ -385,6 +460,9 @@ def main():
                     help="CPU legs time every k-th position (bounded sample)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-rates", default="25,50,100", help="Poisson request rates (req/s)")
+    ap.add_argument("--serve-seconds", type=float, default=8.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -319,20 +319,24 @@ static int end_call(const pg_opts* o)
     return PG_OK;
 }
 
-// batch perft with device inputs; d_out must not alias the inputs
-static int perft_batch_device_locked(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out,
-                                     const pg_opts* o)
+// perft of n roots; each root's count is added to acc[group] (group =
+// groups[i], or i when groups is null).  acc is zeroed first when zero_acc.
+int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc, bool zero_acc,
+               int slider, int block)
 {
     Engine& E = engine();
-    const Variant v = pick_variant(o);
+    pg_opts o{};
+    o.slider = slider;
+    o.block_size = block;
+    const Variant v = pick_variant(&o);
     PG_TRY(ensure_level(0, n));
-    PG_CUDA(cudaMemsetAsync(d_out, 0, (u64)n * sizeof(u64), E.stream));
+    if (zero_acc) PG_CUDA(cudaMemsetAsync(acc, 0, (u64)n * sizeof(u64), E.stream));
     u32* ctr = (u32*)(E.host_scratch + 64);  // pinned, 4 words
     u32* dctr = E.tickets + MAX_TICKETS - 4;
     const u32 init[4] = {0, 0, 0xFFFFFFFFu, 0};
     PG_CUDA(cudaMemcpyAsync(dctr, init, sizeof(init), cudaMemcpyHostToDevice, E.stream));
-    k_partition_roots<<<std::max<u32>(1, std::min<u32>((n + 255) / 256, 4096)), 256, 0, E.stream>>>(d_pos, d_depths, n,
-                                                                                                 E.lv[0].v, dctr);
+    k_partition_roots<<<std::max<u32>(1, std::min<u32>((n + 255) / 256, 4096)), 256, 0, E.stream>>>(
+        d_pos, d_depths, n, E.lv[0].v, dctr, d_groups);
     PG_CUDA(cudaGetLastError());
     E.st.launches++;
     PG_CUDA(cudaMemcpyAsync(ctr, dctr, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
@@ -343,13 +347,75 @@ static int perft_batch_device_locked(const Pos* d_pos, const unsigned char* d_de
         return PG_ERR_INVALID_ARGUMENT;
     }
     cudaEventRecord(E.ev0, E.stream);
-    PG_TRY(run_range(v, 0, 0, nw, 0, (int)mind, (int)maxd, d_out));
-    PG_TRY(run_range(v, 0, nw, n - nw, 1, (int)mind, (int)maxd, d_out));
+    PG_TRY(run_range(v, 0, 0, nw, 0, (int)mind, (int)maxd, acc));
+    PG_TRY(run_range(v, 0, nw, n - nw, 1, (int)mind, (int)maxd, acc));
     cudaEventRecord(E.ev1, E.stream);
     PG_CUDA(cudaEventSynchronize(E.ev1));
     float ms = 0;
     cudaEventElapsedTime(&ms, E.ev0, E.ev1);
     E.st.device_ms = ms;
+    return PG_OK;
+}
+
+// batch perft with device inputs; d_out must not alias the inputs
+static int perft_batch_device_locked(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out,
+                                     const pg_opts* o)
+{
+    return perft_core(d_pos, d_depths, nullptr, n, d_out, true, o ? o->slider : 0, o ? o->block_size : 0);
+}
+
+// The positions `plies` plies below root (all of them, in generateMoves
+// order level by level), written to out as boards; *n_out = their number.
+// Fails with PG_ERR_CAPACITY when they exceed cap or one level buffer.
+int expand_frontier(const Pos& root, int plies, Pos* out, u32 cap, u32* n_out)
+{
+    Engine& E = engine();
+    const Variant v = pick_variant(nullptr);
+    E.ticket_next = 0;
+    PG_CUDA(cudaMemsetAsync(E.tickets, 0, MAX_TICKETS * sizeof(u32), E.stream));
+    PG_CUDA(cudaMemsetAsync(E.err, 0, sizeof(u32), E.stream));
+    PG_TRY(ensure_level(0, 1));
+    PG_TRY(ensure_stage(64));
+    Pos* d_root = (Pos*)E.stage;
+    unsigned char* d_dep = (unsigned char*)E.stage + 48;
+    const unsigned char rem = (unsigned char)(plies + 3);  // >= 3 at every level that is expanded
+    PG_CUDA(cudaMemcpyAsync(d_root, &root, sizeof(Pos), cudaMemcpyHostToDevice, E.stream));
+    PG_CUDA(cudaMemcpyAsync(d_dep, &rem, 1, cudaMemcpyHostToDevice, E.stream));
+    u32* dctr = E.tickets + MAX_TICKETS - 4;
+    const u32 init[4] = {0, 0, 0xFFFFFFFFu, 0};
+    PG_CUDA(cudaMemcpyAsync(dctr, init, sizeof(init), cudaMemcpyHostToDevice, E.stream));
+    k_partition_roots<<<1, 32, 0, E.stream>>>(d_root, d_dep, 1, E.lv[0].v, dctr, nullptr);
+    PG_CUDA(cudaGetLastError());
+    int side = (int)(root.p >> 63);
+    u32 n = 1;
+    for (int L = 0; L < plies; L++) {
+        LevelBuf& lb = E.lv[L];
+        PG_TRY(launch_count(v, side, lb.v, 0, n, lb.cnt));
+        PG_TRY(launch_scan(lb.cnt, n, lb.offs));
+        u64 total = 0;
+        PG_CUDA(cudaMemcpyAsync(E.host_scratch, lb.offs + n, sizeof(u64), cudaMemcpyDeviceToHost, E.stream));
+        PG_CUDA(cudaStreamSynchronize(E.stream));
+        total = E.host_scratch[0];
+        if (total > cap || total > level_cap_max()) {
+            set_error("frontier of %llu positions exceeds the capacity %u", (unsigned long long)total, cap);
+            return PG_ERR_CAPACITY;
+        }
+        if (total == 0) {
+            n = 0;
+            break;
+        }
+        PG_TRY(ensure_level(L + 1, total));
+        PG_TRY(launch_expand(v, side, lb.v, 0, 0, n, lb.offs, E.lv[L + 1].v));
+        n = (u32)total;
+        side ^= 1;
+    }
+    if (n) {
+        k_level_to_boards<<<std::max<u32>(1, std::min<u32>((n + 255) / 256, 4096)), 256, 0, E.stream>>>(
+            E.lv[plies].v, n, out);
+        PG_CUDA(cudaGetLastError());
+    }
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    *n_out = n;
     return PG_OK;
 }
 

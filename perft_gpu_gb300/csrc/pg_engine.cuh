@@ -84,4 +84,9 @@ struct Engine {
 Engine& engine();
 void set_error(const char* fmt, ...);
 
+// engine internals used by the server (call with engine().mu held)
+int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc, bool zero_acc,
+               int slider, int block);
+int expand_frontier(const Pos& root, int plies, Pos* out, u32 cap, u32* n_out);
+
 }  // namespace pg

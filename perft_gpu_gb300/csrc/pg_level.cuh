@@ -21,7 +21,8 @@ __device__ __forceinline__ void store_board(const LevelView& lv, u64 i, const Po
 
 // roots into level 0, white-to-move first, black-to-move from the end
 static __global__ void k_partition_roots(const Pos* __restrict__ in, const unsigned char* __restrict__ depths, u32 n,
-                                  LevelView lv, u32* counters /* [0] white, [1] black, [2] min depth, [3] max depth */)
+                                  LevelView lv, u32* counters /* [0] white, [1] black, [2] min depth, [3] max depth */,
+                                  const u32* __restrict__ groups = nullptr /* group id per root; null = index */)
 {
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const Pos b = in[i];
@@ -30,7 +31,7 @@ static __global__ void k_partition_roots(const Pos* __restrict__ in, const unsig
         if (st_side(b)) slot = n - 1 - atomicAdd(&counters[1], 1u);
         else slot = atomicAdd(&counters[0], 1u);
         store_board(lv, slot, b);
-        lv.grp[slot] = i;
+        lv.grp[slot] = groups ? groups[i] : i;
         lv.rem[slot] = (unsigned char)d;
         atomicMin(&counters[2], d);
         atomicMax(&counters[3], d);
@@ -149,6 +150,12 @@ static __global__ void k_plan(const u64* __restrict__ offs, u32 n, u64 cap, Plan
     if (a < n) atomicOr(err, ERR_PLAN_OVERFLOW);
     plan->nchunks = k;
     plan->total = offs[n];
+}
+
+// level nodes [0, n) of one level buffer into an array of boards
+static __global__ void k_level_to_boards(LevelView lv, u32 n, Pos* __restrict__ out)
+{
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = load_board(lv, i);
 }
 
 }  // namespace pg

@@ -1,0 +1,55 @@
+"""Continuous-batching server: requests of mixed depth submitted while others
+run; each result must equal the reference's golden count and the result of
+the same request computed alone."""
+import time
+
+import numpy as np
+import pytest
+
+from conftest import golden_json, golden_npz, words_of_hex
+
+pytestmark = pytest.mark.gpu
+
+
+def test_server_mixed_requests_match_alone_and_golden(pg):
+    g3 = golden_npz("config3.npz")
+    g2 = golden_json("config2.json")
+    fens = {f["name"]: f for f in golden_json("fens.json")}
+    deep = pg.HexaBitBoardPosition(*words_of_hex(g2["board"]))
+    pos2 = pg.board_from_fen(fens["position2"]["fen"])
+    idx = np.arange(0, 4096, 41)
+    boards = g3["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    srv = pg.Server(hbm_budget_bytes=1 << 30, max_inflight=512)
+    try:
+        want = {}
+        want[srv.submit(deep, 7)] = g2["perft7"]            # deep request first: 8.7e10 leaves
+        for k, i in enumerate(idx[:50]):
+            want[srv.submit(pg.board_of(boards[k]), int(g3["depths"][i]))] = int(g3["totals"][i])
+        time.sleep(0.02)                                      # more arrive while the deep one runs
+        want[srv.submit(pos2, 6)] = fens["position2"]["perft"]["6"] if "6" in fens["position2"]["perft"] else None
+        for k, i in enumerate(idx[50:], start=50):
+            want[srv.submit(pg.board_of(boards[k]), int(g3["depths"][i]))] = int(g3["totals"][i])
+        got = {rid: srv.wait(rid, timeout=300)[0] for rid in want}
+    finally:
+        srv.stop()
+    for rid, w in want.items():
+        if w is not None:
+            assert got[rid] == w, rid
+    # the same requests alone
+    assert pg.perft(pos2, 6) == [v for r, v in got.items() if want[r] is None][0]
+    for k, i in enumerate(idx[:10]):
+        assert pg.perft(pg.board_of(boards[k]), int(g3["depths"][i])) == int(g3["totals"][i])
+
+
+def test_server_rejects_invalid_and_reports_latency(pg):
+    srv = pg.Server(hbm_budget_bytes=64 << 20, max_inflight=4)
+    try:
+        with pytest.raises(pg.PerftError):
+            srv.submit(pg.board_from_fen("8/8/8/8/8/8/8/8 w - - 0 1"), 3)
+        b = pg.board_from_fen("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1")
+        ids = [srv.submit(b, d) for d in (1, 2, 3, 4, 5, 6, 0)]
+        res = [srv.wait(i) for i in ids]
+    finally:
+        srv.stop()
+    assert [r for r, _ in res] == [20, 400, 8902, 197281, 4865609, 119060324, 1]
+    assert all(lat >= 0 for _, lat in res)
