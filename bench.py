@@ -387,12 +387,23 @@ def run_ours(args):
         bytes_per_launch = leaf_nodes * LEAF_PARENT_BYTES / max(leaf_launches, 1)
         achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9 if per_launch_ms else 0.0
         traffic = None
-        tfile = os.path.join(ROOT, "profiles", "k_leaf_traffic.json")
+        alu = None
+        tfile = os.path.join(ROOT, "profiles", "k_leaf_ks_position2_depth6_traffic.json")
         if os.path.exists(tfile):
             with open(tfile) as f:
                 tj = json.load(f)
-            # DRAM bytes per leaf-parent node from the ncu capture, scaled to a launch
+            # DRAM bytes per leaf-parent node from the ncu capture of a smaller
+            # case of the same kernel, scaled to a launch by the nodes it reads
             traffic = tj["dram_bytes_per_leaf_parent"] * leaf_nodes / max(leaf_launches, 1)
+            # integer-ALU roofline: ALU warp instructions per leaf (ncu, same
+            # capture) x leaves per timed step / live k_leaf time
+            leaf_s = leaf_ms / 1e3 / args.steps
+            ach = tj["alu_warp_inst_per_leaf"] * leaves_per_step / leaf_s if leaf_s else 0.0
+            alu = {"bound": "alu", "kernel": "k_leaf", "achieved": ach / 1e9, "peak": tj["alu_peak_warp_inst_per_s"] / 1e9,
+                   "unit": "G warp-inst/s", "frac": ach / tj["alu_peak_warp_inst_per_s"],
+                   "alu_warp_inst_per_leaf": tj["alu_warp_inst_per_leaf"],
+                   "peak_source": "2 ALU warp-instructions/clk/SM x 152 SMs x 2.07 GHz (nominal)",
+                   "source": tj["source"]}
 
         served = None
         if not args.no_serve:
@@ -433,6 +444,7 @@ def run_ours(args):
                          "peak_source": peak_kind,
                          "note": "integer-ALU-bound kernel: algorithmic bytes are the leaf-parent "
                                  "boards read (53 B/node); see roofline_alu"},
+            "roofline_alu": alu,
             "leaf_kernel": {"launches": leaf_launches, "ms_total": leaf_ms,
                             "ms_per_launch": per_launch_ms,
                             "share_of_timed": leaf_ms / (elapsed * 1e3)},
