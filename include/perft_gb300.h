@@ -147,6 +147,11 @@ int pg_perft_batch_device(const pg_board *d_pos, const uint8_t *d_depths, uint32
 int pg_perft_batch_noalloc(const pg_board *d_pos, const uint8_t *d_depths, uint32_t n,
                            uint64_t *d_out, void *stream);
 
+/* Empty the transposition tables (they persist across calls otherwise; an
+ * entry stays valid for its position and remaining depth, so results never
+ * depend on what earlier calls stored).  No counterpart in the reference. */
+int pg_tt_clear(void);
+
 /* ---- inputs ---- */
 /* Seeded random legal playouts from the initial position, generated on the
  * GPU.  Position i is the first accepted attempt a = 0, 1, ... of:

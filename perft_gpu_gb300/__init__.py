@@ -142,6 +142,7 @@ _SIGNATURES = {
     "pg_server_poll": [ctypes.c_uint64, _U64P, ctypes.POINTER(ctypes.c_int),
                        ctypes.POINTER(ctypes.c_double)],
     "pg_server_stop": [],
+    "pg_tt_clear": [],
 }
 
 _lib = None
@@ -292,6 +293,11 @@ def random_playouts(seed: int, n: int, min_plies: int, max_plies: int, min_moves
                                              depth_hi, out.ctypes.data_as(_BP),
                                              depths.ctypes.data_as(_U8P) if with_depths else None))
     return (out, depths) if with_depths else out
+
+
+def tt_clear():
+    """Empty the transposition tables."""
+    _check(load_library().pg_tt_clear())
 
 
 def board_of(row) -> HexaBitBoardPosition:

@@ -59,12 +59,7 @@ void set_error(const char* fmt, ...)
 // launch plans
 // ---------------------------------------------------------------------------
 
-struct Variant {
-    int slider;  // pg_slider (never AUTO here)
-    int T;       // CTA size of the block-queue kernels
-};
-
-static u32* next_ticket()
+u32* next_ticket()
 {
     Engine& E = engine();
     if (E.ticket_next >= MAX_TICKETS - 8) return nullptr;
@@ -78,7 +73,7 @@ static u32* next_ticket()
         return PG_ERR_CAPACITY;                     \
     }
 
-static int launch_leaf(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u64* acc)
+int launch_leaf(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u64* acc)
 {
     Engine& E = engine();
     PG_TICKET(tk);
@@ -89,7 +84,7 @@ static int launch_leaf(const Variant& v, int side, const LevelView& lv, u32 star
     return PG_OK;
 }
 
-static int launch_expand(const Variant& v, int side, const LevelView& in, u32 start, u32 a, u32 b, const u64* offs,
+int launch_expand(const Variant& v, int side, const LevelView& in, u32 start, u32 a, u32 b, const u64* offs,
                          const LevelView& out)
 {
     Engine& E = engine();
@@ -99,7 +94,7 @@ static int launch_expand(const Variant& v, int side, const LevelView& in, u32 st
     return PG_OK;
 }
 
-static int launch_count(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u32* cnt)
+int launch_count(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u32* cnt)
 {
     Engine& E = engine();
     PG_CUDA(ops_for(v.slider).count_level(side, lv, start, n, cnt, E.stream, E.num_sms));
@@ -107,7 +102,7 @@ static int launch_count(const Variant& v, int side, const LevelView& lv, u32 sta
     return PG_OK;
 }
 
-static int launch_scan(const u32* cnt, u32 n, u64* offs)
+int launch_scan(const u32* cnt, u32 n, u64* offs)
 {
     Engine& E = engine();
     const u64 tiles = (n + SCAN_TILE - 1) / SCAN_TILE + 1;
@@ -137,7 +132,7 @@ static int launch_scan(const u32* cnt, u32 n, u64* offs)
 
 static constexpr u64 NODE_BYTES = 48 + 4 + 1 + 4 + 8;
 
-static u64 level_cap_max()
+u64 level_cap_max()
 {
     Engine& E = engine();
     u64 cap = E.budget / NODE_BYTES / 4;
@@ -145,7 +140,7 @@ static u64 level_cap_max()
     return std::max<u64>(cap, 1u << 16);
 }
 
-static int ensure_level(int L, u64 need)
+int ensure_level(int L, u64 need)
 {
     Engine& E = engine();
     if (L >= MAX_LEVELS) {
@@ -244,7 +239,7 @@ static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int mi
     return PG_OK;
 }
 
-static Variant pick_variant(const pg_opts* o)
+Variant pick_variant(const pg_opts* o)
 {
     Engine& E = engine();
     Variant v{PG_SLIDER_KOGGE_STONE, 256};
@@ -279,7 +274,7 @@ static int check_ready()
     return PG_OK;
 }
 
-static int ensure_stage(u64 bytes)
+int ensure_stage(u64 bytes)
 {
     Engine& E = engine();
     if (E.stage_cap >= bytes) return PG_OK;
@@ -628,6 +623,14 @@ int pg_random_playouts(uint64_t seed, uint32_t n, int min_plies, int max_plies, 
     PG_CUDA(cudaMemcpyAsync(out, d, (u64)n * 48, cudaMemcpyDeviceToHost, E.stream));
     if (depths) PG_CUDA(cudaMemcpyAsync(depths, dd, n, cudaMemcpyDeviceToHost, E.stream));
     return end_call(nullptr);
+}
+
+int pg_tt_clear(void)
+{
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    return tt_clear();
 }
 
 int pg_perft_batch_device(const pg_board* d_pos, const uint8_t* d_depths, uint32_t n, uint64_t* d_out,

@@ -84,7 +84,21 @@ struct Engine {
 Engine& engine();
 void set_error(const char* fmt, ...);
 
-// engine internals used by the server (call with engine().mu held)
+// engine internals shared by the translation units (call with engine().mu held)
+struct Variant {
+    int slider;  // pg_slider (never AUTO here)
+    int T;       // CTA size of the block-queue kernels
+};
+Variant pick_variant(const pg_opts* o);
+u32* next_ticket();
+int launch_leaf(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u64* acc);
+int launch_expand(const Variant& v, int side, const LevelView& in, u32 start, u32 a, u32 b, const u64* offs,
+                  const LevelView& out);
+int launch_count(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u32* cnt);
+int launch_scan(const u32* cnt, u32 n, u64* offs);
+u64 level_cap_max();
+int ensure_level(int L, u64 need);
+int ensure_stage(u64 bytes);
 int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc, bool zero_acc,
                int slider, int block);
 int expand_frontier(const Pos& root, int plies, Pos* out, u32 cap, u32* n_out);

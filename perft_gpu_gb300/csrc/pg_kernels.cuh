@@ -220,7 +220,7 @@ __global__ void k_count_level(LevelView lv, u32 start, u32 n, u32* __restrict__ 
     stage_tables<SL>();
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const u32 rem = lv.rem[start + i];
-        cnt[i] = rem >= 3 ? count_moves<S, SL>(load_board(lv, start + i)) : 0u;
+        cnt[i] = (rem >= 3 && rem < REM_DEAD) ? count_moves<S, SL>(load_board(lv, start + i)) : 0u;
     }
 }
 
@@ -294,9 +294,11 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
 
 // children of the nodes [a, b) of a level into the next level; offs is the
 // exclusive scan of the children counts, child slots start at offs[a]
+// parent_out (transposition-table mode): each child's group becomes its own
+// slot and its parent's slot is written to parent_out
 template <int S, class SL, int T, int QCAP>
 __global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32 start, u32 a, u32 b, const u64* __restrict__ offs,
-                                              LevelView out, u32* ticket)
+                                              LevelView out, u32* ticket, u32* __restrict__ parent_out = nullptr)
 {
     extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     stage_tables<SL>();
@@ -344,7 +346,12 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32
                 make_move<S>(ch, (u16)(ent & 0xFFFFu));
                 const u64 o = chunk_out + lo + e;
                 store_board(out, o, ch);
-                out.grp[o] = sg[p];
+                if (parent_out) {
+                    out.grp[o] = (u32)o;
+                    parent_out[o] = (u32)(start + c0 + p);
+                } else {
+                    out.grp[o] = sg[p];
+                }
                 out.rem[o] = (unsigned char)(sr[p] - 1);
             }
             __syncthreads();

@@ -7,6 +7,10 @@
 
 namespace pg {
 
+// remaining-depth value of a node that needs no further work (a
+// transposition-table hit or a duplicate of another node of its level)
+constexpr unsigned char REM_DEAD = 0x80;
+
 __device__ __forceinline__ Pos load_board(const LevelView& lv, u64 i)
 {
     const ulonglong2 a = lv.pl0[i], b = lv.pl1[i], c = lv.pl2[i];

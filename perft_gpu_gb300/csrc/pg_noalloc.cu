@@ -177,7 +177,7 @@ void launch_expand_na(const LevelView& in, u32 start, u32 a, u32 b, const u64* o
     using L = BlockSmem<SlKS, NA_T, Q>;
     auto fn = k_expand<S, SlKS, NA_T, Q>;
     fn<<<grid_of((const void*)fn, NA_T, L::bytes, b - a, sms), NA_T, L::bytes, st>>>(in, start, a, b, offs, out,
-                                                                                      ticket);
+                                                                                      ticket, nullptr);
 }
 
 template <int S>

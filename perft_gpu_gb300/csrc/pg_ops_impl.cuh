@@ -68,7 +68,7 @@ cudaError_t expand_t(const LevelView& in, u32 start, u32 a, u32 b, const u64* of
     static cudaError_t attr = set_smem(fn, L::bytes);
     if (attr) return attr;
     const int grid = occupancy_grid((const void*)fn, T, L::bytes, (u64)(b - a), sms);
-    fn<<<grid, T, L::bytes, st>>>(in, start, a, b, offs, out, ticket);
+    fn<<<grid, T, L::bytes, st>>>(in, start, a, b, offs, out, ticket, nullptr);
     return cudaGetLastError();
 }
 

@@ -1,14 +1,438 @@
-// pg_tt.cu -- transposition-table perft.
+// pg_tt.cu -- perft with Zobrist transposition tables in HBM.
+//
+// The reference's TT path (perft_bb_gpu_simple_hash, perft_bb.h:1242-1589;
+// entries chess.h:410-504; probes perft_bb.h:664-761; duplicate marking
+// perft_bb.h:790-852; upsweep and stores perft_bb.h:854-961) re-planned for
+// the chunked breadth-first driver:
+//   * keys: 781 seeded 64-bit Zobrist numbers (piece-square x 768, castling
+//     rights x 4, en-passant file x 8, side to move), a fresh seeded set
+//     rather than the reference's randoms.cpp (counts do not depend on keys);
+//   * one table per remaining depth 2..9, 16-byte entries {key ^ count,
+//     count} written with one 16-byte store and accepted only when the XOR of
+//     the two words equals the probing key, so a torn or foreign entry is a
+//     miss, never a wrong count (the reference's lockless XOR scheme);
+//   * per level: probe (a hit resolves the node), duplicate detection inside
+//     the level (first claim in a level table; later equal keys take the
+//     claimant's count), the usual leaf / count / scan / expand for the live
+//     nodes, and after each chunk an upsweep that stores the children's final
+//     counts and adds them into their parents.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "pg_kernels.cuh"
+#include "pg_tables.h"
 #include "pg_tt.cuh"
 
 namespace pg {
 
-void tt_free() {}
+constexpr int ZOBRIST_KEYS = 781;
+constexpr int Z_CASTLE = 768, Z_EP = 772, Z_SIDE = 780;
+constexpr int TT_MIN_DEPTH = 2, TT_MAX_DEPTH = 9;
+constexpr u32 NO_DUP = 0xFFFFFFFFu;
 
-int tt_perft_batch_device(const Pos*, const unsigned char*, u32, u64*, const pg_opts*)
+static __device__ u64 g_zobrist[ZOBRIST_KEYS];
+
+struct TTSet {
+    ulonglong2* tab[16];
+    u64 mask[16];
+};
+
+struct LevelTT {
+    u64* hash = nullptr;
+    u64* acc = nullptr;
+    u32* parent = nullptr;
+    u32* dup = nullptr;
+    u64* dd_hash = nullptr;  // duplicate table of the level
+    u32* dd_idx = nullptr;
+    u64 cap = 0, dd_cap = 0;
+    void* block = nullptr;
+};
+
+struct TTState {
+    bool keys_ready = false;
+    TTSet set{};
+    void* pool = nullptr;
+    u64 pool_bytes = 0;
+    LevelTT lv[MAX_LEVELS];
+    u32* root_of = nullptr;
+    u64 root_cap = 0;
+    u64* counters = nullptr;  // probes, hits, stores
+};
+static TTState g_tt;
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ u64 zobrist_hash(const Pos& b)
 {
-    set_error("transposition tables are not built yet");
-    return PG_ERR_INVALID_ARGUMENT;
+    const u64 pawns = b.p & INNER;
+    const u64 sets[6] = {pawns, b.n, b.bq & ~b.rq, b.rq & ~b.bq, b.bq & b.rq, b.k};
+    u64 h = 0;
+#pragma unroll
+    for (int t = 0; t < 6; t++) {
+        for (u64 s = sets[t] & b.w; s; s &= s - 1) h ^= __ldg(&g_zobrist[t * 64 + lsb(s)]);
+        for (u64 s = sets[t] & ~b.w; s; s &= s - 1) h ^= __ldg(&g_zobrist[(6 + t) * 64 + lsb(s)]);
+    }
+    const int wc = st_wc(b), bc = st_bc(b), ep = st_ep(b);
+    if (wc & 1) h ^= __ldg(&g_zobrist[Z_CASTLE + 0]);
+    if (wc & 2) h ^= __ldg(&g_zobrist[Z_CASTLE + 1]);
+    if (bc & 1) h ^= __ldg(&g_zobrist[Z_CASTLE + 2]);
+    if (bc & 2) h ^= __ldg(&g_zobrist[Z_CASTLE + 3]);
+    if (ep) h ^= __ldg(&g_zobrist[Z_EP + ((ep - 1) & 7)]);
+    if (st_side(b)) h ^= __ldg(&g_zobrist[Z_SIDE]);
+    return h ? h : 1;  // 0 marks an empty slot of the duplicate table
+}
+
+// the duplicate key includes the remaining depth: one level of a mixed-depth
+// batch can hold the same position at different depths
+__device__ __forceinline__ u64 dd_key(u64 h, u32 rem)
+{
+    const u64 k = h ^ (0x9E3779B97F4A7C15ull * (rem + 1));
+    return k ? k : 1;
+}
+__device__ __forceinline__ u32 dd_slot(u64 k, u64 mask) { return (u32)(((k >> 23) ^ (k >> 41) ^ k) & mask); }
+
+// hash, TT probe, and first claim of the level's duplicate table
+static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TTSet tt, u64 dd_mask, u64* counters)
+{
+    u64 probes = 0, hits = 0;
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const u32 idx = start + i;
+        const u32 rem = lv.rem[idx];
+        lt.acc[idx] = 0;
+        lt.dup[idx] = NO_DUP;
+        if (rem < TT_MIN_DEPTH || rem >= REM_DEAD) continue;
+        const u64 h = zobrist_hash(load_board(lv, idx));
+        lt.hash[idx] = h;
+        if (rem <= TT_MAX_DEPTH && tt.tab[rem]) {
+            probes++;
+            const ulonglong2 e = tt.tab[rem][h & tt.mask[rem]];
+            if ((e.x ^ e.y) == h) {
+                lt.acc[idx] = e.y;
+                lv.rem[idx] = REM_DEAD;
+                hits++;
+                continue;
+            }
+        }
+        const u64 k = dd_key(h, rem);
+        const u32 s = dd_slot(k, dd_mask);
+        const u64 prev = atomicCAS(&lt.dd_hash[s], 0ull, k);
+        if (prev == 0 || prev == k) atomicMin(&lt.dd_idx[s], idx);
+    }
+    if (probes) atomicAdd(&counters[0], probes);
+    if (hits) atomicAdd(&counters[1], hits);
+}
+
+// a node whose key was claimed first by another node of its level takes that
+// node's count later and does no work itself
+static __global__ void k_tt_dedup(LevelView lv, u32 start, u32 n, LevelTT lt, u64 dd_mask)
+{
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const u32 idx = start + i;
+        const u32 rem = lv.rem[idx];
+        if (rem < TT_MIN_DEPTH || rem >= REM_DEAD) continue;
+        const u64 k = dd_key(lt.hash[idx], rem);
+        const u32 s = dd_slot(k, dd_mask);
+        if (lt.dd_hash[s] == k) {
+            const u32 rep = lt.dd_idx[s];
+            if (rep != idx) {
+                lt.dup[idx] = rep;
+                lv.rem[idx] = REM_DEAD;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tt_store(const TTSet& tt, u32 rem, u64 h, u64 v)
+{
+    // one 16-byte store: {key ^ count, count}
+    tt.tab[rem][h & tt.mask[rem]] = make_ulonglong2(h ^ v, v);
+}
+
+// children [0, m) of one chunk are final: store them and add them to parents
+static __global__ void k_tt_upsweep(LevelView ch, u32 m, LevelTT ct, TTSet tt, u64* __restrict__ parent_acc,
+                                    u64* counters)
+{
+    u64 stores = 0;
+    for (u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+        const u32 d = ct.dup[j];
+        const u64 v = d != NO_DUP ? ct.acc[d] : ct.acc[j];
+        const u32 rem = ch.rem[j];
+        if (rem >= TT_MIN_DEPTH && rem <= TT_MAX_DEPTH && tt.tab[rem]) {
+            tt_store(tt, rem, ct.hash[j], v);
+            stores++;
+        }
+        atomicAdd(&parent_acc[ct.parent[j]], v);
+    }
+    if (stores) atomicAdd(&counters[2], stores);
+}
+
+// level 0: remember each slot's root, make each slot its own group
+static __global__ void k_tt_roots(LevelView lv, u32 n, u32* __restrict__ root_of)
+{
+    for (u32 s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        root_of[s] = lv.grp[s];
+        lv.grp[s] = s;
+    }
+}
+
+static __global__ void k_tt_finish(LevelView lv, u32 n, LevelTT lt, TTSet tt, const u32* __restrict__ root_of,
+                                   u64* __restrict__ out, u64* counters)
+{
+    u64 stores = 0;
+    for (u32 s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const u32 d = lt.dup[s];
+        const u64 v = d != NO_DUP ? lt.acc[d] : lt.acc[s];
+        const u32 rem = lv.rem[s];
+        if (rem >= TT_MIN_DEPTH && rem <= TT_MAX_DEPTH && tt.tab[rem]) {
+            tt_store(tt, rem, lt.hash[s], v);
+            stores++;
+        }
+        out[root_of[s]] = v;
+    }
+    if (stores) atomicAdd(&counters[2], stores);
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+
+#define TT_CUDA(call)                                                                        \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return e_ == cudaErrorMemoryAllocation ? PG_ERR_OUT_OF_MEMORY : PG_ERR_CUDA;    \
+        }                                                                                    \
+    } while (0)
+#define TT_TRY(expr)                  \
+    do {                              \
+        int r_ = (expr);              \
+        if (r_ != PG_OK) return r_;   \
+    } while (0)
+
+static int small_grid(u64 n) { return (int)std::max<u64>(1, std::min<u64>((n + 255) / 256, 8192)); }
+
+int tt_upload_keys()
+{
+    // 781 keys from splitmix64 with a fixed seed
+    u64 keys[ZOBRIST_KEYS];
+    u64 s = 0x5EED2B1D0C0FFEE5ull;
+    for (int i = 0; i < ZOBRIST_KEYS; i++) {
+        u64 z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        keys[i] = z ^ (z >> 31);
+    }
+    TT_CUDA(cudaMemcpyToSymbol(g_zobrist, keys, sizeof(keys)));
+    const HostTables* t = host_tables();
+    if (!t) {
+        set_error("table construction failed");
+        return PG_ERR_CUDA;
+    }
+    TT_CUDA(cudaMemcpyToSymbol(g_knight, t->knight, sizeof(t->knight)));
+    g_tt.keys_ready = true;
+    return PG_OK;
+}
+
+static int ensure_tables(u64 bytes)
+{
+    Engine& E = engine();
+    if (g_tt.pool && g_tt.pool_bytes == bytes) return PG_OK;
+    if (g_tt.pool) {
+        cudaFree(g_tt.pool);
+        g_tt.pool = nullptr;
+        g_tt.set = TTSet{};
+    }
+    const int ntab = TT_MAX_DEPTH - TT_MIN_DEPTH + 1;
+    u64 entries = 1;
+    while (entries * 2 * 16 * ntab <= bytes) entries *= 2;
+    if (entries < 1024) {
+        set_error("transposition-table budget of %llu bytes is too small", (unsigned long long)bytes);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    TT_CUDA(cudaMalloc(&g_tt.pool, entries * 16 * ntab));
+    TT_CUDA(cudaMemsetAsync(g_tt.pool, 0, entries * 16 * ntab, E.stream));
+    g_tt.pool_bytes = bytes;
+    for (int d = TT_MIN_DEPTH; d <= TT_MAX_DEPTH; d++) {
+        g_tt.set.tab[d] = (ulonglong2*)g_tt.pool + (u64)(d - TT_MIN_DEPTH) * entries;
+        g_tt.set.mask[d] = entries - 1;
+    }
+    if (!g_tt.counters) TT_CUDA(cudaMalloc(&g_tt.counters, 4 * sizeof(u64)));
+    return PG_OK;
+}
+
+static int ensure_level_tt(int L, u64 need)
+{
+    LevelTT& t = g_tt.lv[L];
+    if (t.cap >= need) return PG_OK;
+    if (t.block) {
+        TT_CUDA(cudaStreamSynchronize(engine().stream));
+        cudaFree(t.block);
+        t = LevelTT{};
+    }
+    u64 cap = 1 << 16;
+    while (cap < need) cap <<= 1;
+    const u64 dd = cap * 2;
+    const u64 bytes = cap * (8 + 8 + 4 + 4) + dd * (8 + 4) + 1024;
+    void* blk = nullptr;
+    cudaError_t e = cudaMalloc(&blk, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("transposition-table level %d of %llu nodes failed: %s", L, (unsigned long long)cap,
+                  cudaGetErrorString(e));
+        return PG_ERR_OUT_OF_MEMORY;
+    }
+    unsigned char* p = (unsigned char*)blk;
+    t.hash = (u64*)p;
+    p += cap * 8;
+    t.acc = (u64*)p;
+    p += cap * 8;
+    t.dd_hash = (u64*)p;
+    p += dd * 8;
+    t.parent = (u32*)p;
+    p += cap * 4;
+    t.dup = (u32*)p;
+    p += cap * 4;
+    t.dd_idx = (u32*)p;
+    t.cap = cap;
+    t.dd_cap = dd;
+    t.block = blk;
+    return PG_OK;
+}
+
+static int run_range_tt(const Variant& v, int L, u32 start, u32 n, int side, int minrem, int maxrem)
+{
+    Engine& E = engine();
+    if (n == 0) return PG_OK;
+    LevelBuf& lb = E.lv[L];
+    LevelTT& lt = g_tt.lv[L];
+    u64 dd = 1024;
+    while (dd < 2ull * n) dd <<= 1;
+    dd = std::min(dd, lt.dd_cap);
+    TT_CUDA(cudaMemsetAsync(lt.dd_hash, 0, dd * 8, E.stream));
+    TT_CUDA(cudaMemsetAsync(lt.dd_idx, 0xFF, dd * 4, E.stream));
+    k_tt_probe<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, g_tt.set, dd - 1, g_tt.counters);
+    k_tt_dedup<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, dd - 1);
+    TT_CUDA(cudaGetLastError());
+    E.st.launches += 2;
+    if (minrem <= 2) TT_TRY(launch_leaf(v, side, lb.v, start, n, lt.acc));
+    if (maxrem < 3) return PG_OK;
+    TT_TRY(launch_count(v, side, lb.v, start, n, lb.cnt));
+    TT_TRY(launch_scan(lb.cnt, n, lb.offs));
+    const u64 cap_next = level_cap_max();
+    k_plan<<<1, 32, 0, E.stream>>>(lb.offs, n, cap_next, E.plan_dev, E.err);
+    TT_CUDA(cudaGetLastError());
+    TT_CUDA(cudaMemcpyAsync(E.plan_host, E.plan_dev, sizeof(PlanOut), cudaMemcpyDeviceToHost, E.stream));
+    TT_CUDA(cudaStreamSynchronize(E.stream));
+    const PlanOut plan = *E.plan_host;
+    std::vector<u32> bnd(plan.bnd, plan.bnd + plan.nchunks + 1);
+    std::vector<u64> boff(plan.coff, plan.coff + plan.nchunks + 1);
+    const int cminrem = std::max(minrem, 3) - 1, cmaxrem = maxrem - 1;
+    for (size_t k = 0; k + 1 < bnd.size(); k++) {
+        const u64 children = boff[k + 1] - boff[k];
+        if (!children) continue;
+        TT_TRY(ensure_level(L + 1, children));
+        TT_TRY(ensure_level_tt(L + 1, children));
+        u32* tk = next_ticket();
+        if (!tk) {
+            set_error("dynamic-scheduling counters exhausted");
+            return PG_ERR_CAPACITY;
+        }
+        constexpr int T = 256, Q = T * 32;
+        using BL = BlockSmem<SlKS, T, Q>;
+        const int grid = std::min<u64>((bnd[k + 1] - bnd[k] + T - 1) / T, (u64)E.num_sms * 2);
+        if (side)
+            k_expand<1, SlKS, T, Q><<<std::max(grid, 1), T, BL::bytes, E.stream>>>(
+                lb.v, start, bnd[k], bnd[k + 1], lb.offs, E.lv[L + 1].v, tk, g_tt.lv[L + 1].parent);
+        else
+            k_expand<0, SlKS, T, Q><<<std::max(grid, 1), T, BL::bytes, E.stream>>>(
+                lb.v, start, bnd[k], bnd[k + 1], lb.offs, E.lv[L + 1].v, tk, g_tt.lv[L + 1].parent);
+        TT_CUDA(cudaGetLastError());
+        E.st.launches++;
+        TT_TRY(run_range_tt(v, L + 1, 0, (u32)children, 1 - side, cminrem, cmaxrem));
+        k_tt_upsweep<<<small_grid(children), 256, 0, E.stream>>>(E.lv[L + 1].v, (u32)children, g_tt.lv[L + 1],
+                                                                 g_tt.set, lt.acc, g_tt.counters);
+        TT_CUDA(cudaGetLastError());
+        E.st.launches++;
+    }
+    return PG_OK;
+}
+
+void tt_free()
+{
+    if (g_tt.pool) cudaFree(g_tt.pool);
+    for (auto& t : g_tt.lv) {
+        if (t.block) cudaFree(t.block);
+        t = LevelTT{};
+    }
+    if (g_tt.root_of) cudaFree(g_tt.root_of);
+    if (g_tt.counters) cudaFree(g_tt.counters);
+    g_tt = TTState{};
+}
+
+int tt_clear()
+{
+    Engine& E = engine();
+    if (g_tt.pool) {
+        const u64 bytes = (g_tt.set.mask[TT_MIN_DEPTH] + 1) * 16ull * (TT_MAX_DEPTH - TT_MIN_DEPTH + 1);
+        TT_CUDA(cudaMemsetAsync(g_tt.pool, 0, bytes, E.stream));
+    }
+    TT_CUDA(cudaStreamSynchronize(E.stream));
+    return PG_OK;
+}
+
+int tt_perft_batch_device(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out, const pg_opts* o)
+{
+    Engine& E = engine();
+    if (!g_tt.keys_ready) TT_TRY(tt_upload_keys());
+    u64 bytes = (o && o->tt_bytes) ? o->tt_bytes : std::min<u64>(32ull << 30, E.budget / 4);
+    TT_TRY(ensure_tables(bytes));
+    const Variant v = pick_variant(o);
+    TT_TRY(ensure_level(0, n));
+    TT_TRY(ensure_level_tt(0, n));
+    if (g_tt.root_cap < n) {
+        if (g_tt.root_of) cudaFree(g_tt.root_of);
+        g_tt.root_of = nullptr;
+        TT_CUDA(cudaMalloc(&g_tt.root_of, (u64)n * 4));
+        g_tt.root_cap = n;
+    }
+    TT_CUDA(cudaMemsetAsync(g_tt.counters, 0, 4 * sizeof(u64), E.stream));
+    u32* ctr = (u32*)(E.host_scratch + 64);
+    u32* dctr = E.tickets + MAX_TICKETS - 4;
+    const u32 init[4] = {0, 0, 0xFFFFFFFFu, 0};
+    TT_CUDA(cudaMemcpyAsync(dctr, init, sizeof(init), cudaMemcpyHostToDevice, E.stream));
+    k_partition_roots<<<small_grid(n), 256, 0, E.stream>>>(d_pos, d_depths, n, E.lv[0].v, dctr, nullptr);
+    k_tt_roots<<<small_grid(n), 256, 0, E.stream>>>(E.lv[0].v, n, g_tt.root_of);
+    TT_CUDA(cudaGetLastError());
+    TT_CUDA(cudaMemcpyAsync(ctr, dctr, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+    TT_CUDA(cudaStreamSynchronize(E.stream));
+    const u32 nw = ctr[0], mind = ctr[2], maxd = ctr[3];
+    if (maxd > 15) {
+        set_error("depth %u out of range 0..15", maxd);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    cudaEventRecord(E.ev0, E.stream);
+    TT_TRY(run_range_tt(v, 0, 0, nw, 0, (int)mind, (int)maxd));
+    TT_TRY(run_range_tt(v, 0, nw, n - nw, 1, (int)mind, (int)maxd));
+    k_tt_finish<<<small_grid(n), 256, 0, E.stream>>>(E.lv[0].v, n, g_tt.lv[0], g_tt.set, g_tt.root_of, d_out,
+                                                     g_tt.counters);
+    TT_CUDA(cudaGetLastError());
+    cudaEventRecord(E.ev1, E.stream);
+    u64 c[4];
+    TT_CUDA(cudaMemcpyAsync(c, g_tt.counters, sizeof(c), cudaMemcpyDeviceToHost, E.stream));
+    TT_CUDA(cudaEventSynchronize(E.ev1));
+    TT_CUDA(cudaStreamSynchronize(E.stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+    E.st.device_ms = ms;
+    E.st.tt_probes = c[0];
+    E.st.tt_hits = c[1];
+    E.st.tt_stores = c[2];
+    return PG_OK;
 }
 
 }  // namespace pg

@@ -5,6 +5,7 @@
 namespace pg {
 
 void tt_free();
+int tt_clear();
 int tt_perft_batch_device(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out, const pg_opts* o);
 
 }  // namespace pg

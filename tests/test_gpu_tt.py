@@ -1,0 +1,61 @@
+"""Transposition-table perft: every count equals the reference's golden count
+and the no-TT count, also when a tiny table forces constant overwrites."""
+import numpy as np
+import pytest
+
+from conftest import golden_json, golden_npz, words_of_hex
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tt_reference_fens(pg):
+    pg.tt_clear()
+    for item in golden_json("fens.json"):
+        b = pg.board_from_fen(item["fen"])
+        for d, v in item["perft"].items():
+            if int(d) <= 5:
+                assert pg.perft(b, int(d), use_tt=True) == v, (item["name"], d)
+
+
+def test_tt_config4_depth5_and_stats(pg):
+    g = golden_npz("config4_d5.npz")
+    boards = g["boards"].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    pg.tt_clear()
+    st = pg.PgStats()
+    out = pg.perft_batch(boards, [5] * len(boards), use_tt=True, stats=st)
+    assert np.array_equal(out, g["totals"])
+    # breadth-first: a level is probed before any of it is stored, so a cold
+    # single pass stores but finds transpositions through the level's
+    # duplicate pass instead; the second pass hits the stored entries
+    assert st.tt_probes > 0 and st.tt_stores > 0
+    st2 = pg.PgStats()
+    out2 = pg.perft_batch(boards, [5] * len(boards), use_tt=True, stats=st2)
+    assert np.array_equal(out2, g["totals"])
+    assert st2.tt_hits > 0
+
+
+def test_tt_equals_no_tt_on_batched_workload(pg):
+    g = golden_npz("config3.npz")
+    idx = np.arange(0, 4096, 5)
+    boards = g["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    depths = np.minimum(g["depths"][idx], 5)
+    pg.tt_clear()
+    assert np.array_equal(pg.perft_batch(boards, depths, use_tt=True), pg.perft_batch(boards, depths))
+
+
+def test_tt_tiny_table_and_duplicate_roots(pg):
+    fens = {f["name"]: f for f in golden_json("fens.json")}
+    b = pg.board_from_fen(fens["position2"]["fen"])
+    boards = pg.boards_array([b, b, pg.board_from_fen(fens["start"]["fen"]), b])
+    out = pg.perft_batch(boards, [4, 4, 5, 3], use_tt=True, tt_bytes=1 << 20)
+    assert [int(x) for x in out] == [fens["position2"]["perft"]["4"]] * 2 + [fens["start"]["perft"]["5"],
+                                                                              fens["position2"]["perft"]["3"]]
+    pg.tt_clear()
+
+
+def test_tt_config2_depth7(pg):
+    g = golden_json("config2.json")
+    b = pg.HexaBitBoardPosition(*words_of_hex(g["board"]))
+    pg.tt_clear()
+    assert pg.perft(b, 7, use_tt=True) == g["perft7"]
+    assert pg.perft(b, 6, use_tt=True) == g["perft6"]
