@@ -147,6 +147,21 @@ int pg_perft_batch_device(const pg_board *d_pos, const uint8_t *d_depths, uint32
 int pg_perft_batch_noalloc(const pg_board *d_pos, const uint8_t *d_depths, uint32_t n,
                            uint64_t *d_out, void *stream);
 
+/* The autotuner's choices (it runs once, on the first call that leaves slider,
+ * block size and switch depth at 0, or here).  Per root depth d: the slider
+ * policy and CTA size of the leaf kernel and the calibration rate in leaf
+ * nodes/s (depths 3..6 measured; shallower/deeper copy the ends).
+ * leaf_plies is the switch depth: plies finished inside one CTA.  No
+ * counterpart in the reference (its switches are compile-time, switches.h). */
+typedef struct pg_tuning {
+    int leaf_plies;
+    int slider[16];
+    int block_size[16];
+    double leaves_per_s[16];
+    double seconds;
+} pg_tuning;
+int pg_autotune(pg_tuning *out);
+
 /* Empty the transposition tables (they persist across calls otherwise; an
  * entry stays valid for its position and remaining depth, so results never
  * depend on what earlier calls stored).  No counterpart in the reference. */

@@ -108,6 +108,20 @@ class PgOpts(ctypes.Structure):
                 ("stats", ctypes.POINTER(PgStats))]
 
 
+class PgTuning(ctypes.Structure):
+    _fields_ = [("leaf_plies", ctypes.c_int), ("slider", ctypes.c_int * 16),
+                ("block_size", ctypes.c_int * 16), ("leaves_per_s", ctypes.c_double * 16),
+                ("seconds", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        names = {v: k for k, v in SLIDERS.items()}
+        return {"leaf_plies": self.leaf_plies, "seconds": self.seconds,
+                "per_depth": {d: {"slider": names.get(self.slider[d], self.slider[d]),
+                                  "block_size": self.block_size[d],
+                                  "calibration_leaves_per_s": self.leaves_per_s[d]}
+                              for d in range(3, 7)}}
+
+
 class PgServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
                 ("slider", ctypes.c_int), ("max_wave_nodes", ctypes.c_uint32)]
@@ -143,6 +157,7 @@ _SIGNATURES = {
                        ctypes.POINTER(ctypes.c_double)],
     "pg_server_stop": [],
     "pg_tt_clear": [],
+    "pg_autotune": [ctypes.POINTER(PgTuning)],
 }
 
 _lib = None
@@ -176,10 +191,11 @@ def _check(status: int):
         raise PerftError(status, load_library().pg_last_error().decode(errors="replace"))
 
 
-def _opts(slider=None, block_size=0, use_tt=False, tt_bytes=0, graph=False, stats=None):
+def _opts(slider=None, block_size=0, use_tt=False, tt_bytes=0, graph=False, stats=None, leaf_plies=0):
     o = PgOpts()
     o.slider = SLIDERS[slider] if isinstance(slider, str) else (slider or 0)
     o.block_size = block_size
+    o.leaf_plies = leaf_plies
     o.use_tt = 1 if use_tt else 0
     o.tt_bytes = tt_bytes
     o.graph = 1 if graph else 0
@@ -293,6 +309,13 @@ def random_playouts(seed: int, n: int, min_plies: int, max_plies: int, min_moves
                                              depth_hi, out.ctypes.data_as(_BP),
                                              depths.ctypes.data_as(_U8P) if with_depths else None))
     return (out, depths) if with_depths else out
+
+
+def autotune() -> dict:
+    """Run (once) and report the autotuner's per-depth choices."""
+    t = PgTuning()
+    _check(load_library().pg_autotune(ctypes.byref(t)))
+    return t.as_dict()
 
 
 def tt_clear():

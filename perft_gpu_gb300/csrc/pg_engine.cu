@@ -77,7 +77,7 @@ int launch_leaf(const Variant& v, int side, const LevelView& lv, u32 start, u32 
 {
     Engine& E = engine();
     PG_TICKET(tk);
-    PG_CUDA(ops_for(v.slider).leaf(side, v.T, lv, start, n, acc, tk, E.stream, E.num_sms));
+    PG_CUDA(ops_for(v.slider).leaf(side, v.T, lv, start, n, acc, tk, (u32)v.leaf_plies, E.stream, E.num_sms));
     E.st.launches++;
     E.st.leaf_kernel_launches++;
     E.st.leaf_parent_nodes += n;
@@ -97,7 +97,7 @@ int launch_expand(const Variant& v, int side, const LevelView& in, u32 start, u3
 int launch_count(const Variant& v, int side, const LevelView& lv, u32 start, u32 n, u32* cnt)
 {
     Engine& E = engine();
-    PG_CUDA(ops_for(v.slider).count_level(side, lv, start, n, cnt, E.stream, E.num_sms));
+    PG_CUDA(ops_for(v.slider).count_level(side, lv, start, n, cnt, (u32)v.leaf_plies + 1, E.stream, E.num_sms));
     E.st.launches++;
     return PG_OK;
 }
@@ -192,23 +192,38 @@ int ensure_level(int L, u64 need)
 // breadth-first driver
 // ---------------------------------------------------------------------------
 
+// the leaf kernel's variant at level L: nodes finishing there come from roots
+// of depth L + leaf_plies, and the tuner picked a variant per root depth
+static Variant leaf_variant(const Variant& v, int L)
+{
+    Engine& E = engine();
+    if (!v.per_depth || !E.tuned) return v;
+    Variant w = v;
+    const int d = std::min(L + v.leaf_plies, 15);
+    if (E.tuned_slider[d]) {
+        w.slider = E.tuned_slider[d];
+        w.T = E.tuned_T[d];
+    }
+    return w;
+}
+
 static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int minrem, int maxrem, u64* acc)
 {
     Engine& E = engine();
     if (n == 0) return PG_OK;
     LevelBuf& lb = E.lv[L];
     E.st.peak_level_bytes = std::max<uint64_t>(E.st.peak_level_bytes, (uint64_t)n * 48);
-    if (minrem <= 2) {
+    const int lp = v.leaf_plies;
+    if (minrem <= lp) {
         cudaEventRecord(E.lev0, E.stream);
-        PG_TRY(launch_leaf(v, side, lb.v, start, n, acc));
+        PG_TRY(launch_leaf(leaf_variant(v, L), side, lb.v, start, n, acc));
         cudaEventRecord(E.lev1, E.stream);
-        // the leaf kernel's time is read back at the next sync
         float ms = 0;
         PG_CUDA(cudaEventSynchronize(E.lev1));
         cudaEventElapsedTime(&ms, E.lev0, E.lev1);
         E.st.leaf_kernel_ms += ms;
     }
-    if (maxrem < 3) return PG_OK;
+    if (maxrem <= lp) return PG_OK;
     PG_TRY(launch_count(v, side, lb.v, start, n, lb.cnt));
     PG_TRY(launch_scan(lb.cnt, n, lb.offs));
     const u64 cap_next = level_cap_max();
@@ -227,7 +242,7 @@ static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int mi
     std::vector<u32> bnd(plan.bnd, plan.bnd + plan.nchunks + 1);
     if (plan.total == 0) return PG_OK;
     std::vector<u64> boff(plan.coff, plan.coff + plan.nchunks + 1);
-    const int cminrem = std::max(minrem, 3) - 1, cmaxrem = maxrem - 1;
+    const int cminrem = std::max(minrem, lp + 1) - 1, cmaxrem = maxrem - 1;
     for (size_t k = 0; k + 1 < bnd.size(); k++) {
         const u32 a = bnd[k], b = bnd[k + 1];
         const u64 children = boff[k + 1] - boff[k];
@@ -239,15 +254,115 @@ static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int mi
     return PG_OK;
 }
 
+// The autotuner: per root depth 3..6, a seeded calibration batch is timed
+// with each candidate leaf variant (slider policy x CTA size); the fastest
+// serves that depth (shallower depths take depth 3's, deeper ones depth 6's).
+// The switch depth (last one or two plies inside the CTA) is chosen on the
+// depth-5 batch.  Runs once per engine, on the first call that leaves the
+// choice to it; its own buffers, so a caller's staged inputs are untouched.
+static int autotune_locked()
+{
+    Engine& E = engine();
+    if (E.tuned) return PG_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    const pg_stats saved = E.st;
+    struct Cal {
+        int depth;
+        u32 n;
+    };
+    const Cal cals[] = {{3, 2048}, {4, 512}, {5, 64}, {6, 4}};
+    const int cand[][2] = {{PG_SLIDER_KOGGE_STONE, 128}, {PG_SLIDER_KOGGE_STONE, 256}, {PG_SLIDER_KOGGE_STONE, 512},
+                           {PG_SLIDER_FANCY, 256},        {PG_SLIDER_FANCY, 512},        {PG_SLIDER_BYTE_SMEM, 512}};
+    const u32 nmax = 2048;
+    void* buf = nullptr;
+    PG_CUDA(cudaMalloc(&buf, nmax * (48 + 1 + 8) + 256));
+    Pos* d_pos = (Pos*)buf;
+    unsigned char* d_dep = (unsigned char*)buf + nmax * 48;
+    u64* d_out = (u64*)(((uintptr_t)(d_dep + nmax) + 15) & ~(uintptr_t)15);
+    pg_board start;
+    pg_board_from_fen("rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1", &start);
+    Pos sp;
+    memcpy(&sp, &start, sizeof(sp));
+    int rc = PG_OK;
+    auto time_run = [&](const Cal& c, const Variant& v, double& best) {
+        for (int rep = 0; rep < 2 && rc == PG_OK; rep++) {
+            rc = perft_core(d_pos, d_dep, nullptr, c.n, d_out, true, v);
+            if (rc == PG_OK && E.st.device_ms > 0) best = std::min(best, E.st.device_ms);
+        }
+    };
+    for (const Cal& c : cals) {
+        if (rc != PG_OK) break;
+        cudaError_t e = g_ops_ks.playouts(sp, 0x7E57ull + c.depth, c.n, 0, 60, 1, c.depth, c.depth, d_pos, d_dep,
+                                          E.err, E.stream);
+        if (e != cudaSuccess) {
+            rc = PG_ERR_CUDA;
+            break;
+        }
+        double best_ms = 1e30;
+        int best = 1;
+        for (int k = 0; k < 6 && rc == PG_OK; k++) {
+            Variant v;
+            v.slider = cand[k][0];
+            v.T = cand[k][1];
+            double ms = 1e30;
+            time_run(c, v, ms);
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = k;
+            }
+        }
+        u64 leaves = 0;
+        std::vector<u64> out(c.n);
+        if (rc == PG_OK && cudaMemcpy(out.data(), d_out, c.n * 8, cudaMemcpyDeviceToHost) == cudaSuccess)
+            for (u64 x : out) leaves += x;
+        E.tuned_slider[c.depth] = cand[best][0];
+        E.tuned_T[c.depth] = cand[best][1];
+        E.tuned_rate[c.depth] = best_ms < 1e29 ? leaves / (best_ms * 1e-3) : 0;
+        if (c.depth == 5 && rc == PG_OK) {  // switch depth on the depth-5 batch
+            Variant v;
+            v.slider = cand[best][0];
+            v.T = cand[best][1];
+            v.leaf_plies = 1;
+            double ms1 = 1e30;
+            time_run(c, v, ms1);
+            E.tuned_leaf_plies = ms1 < best_ms ? 1 : 2;
+        }
+    }
+    cudaFree(buf);
+    if (rc != PG_OK) return rc;
+    for (int d = 0; d < 3; d++) {
+        E.tuned_slider[d] = E.tuned_slider[3];
+        E.tuned_T[d] = E.tuned_T[3];
+    }
+    for (int d = 7; d < 16; d++) {
+        E.tuned_slider[d] = E.tuned_slider[6];
+        E.tuned_T[d] = E.tuned_T[6];
+    }
+    E.st = saved;
+    E.tuned = true;
+    E.tune_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return PG_OK;
+}
+
+// resolves the options to a launch variant; slider, block size and switch
+// depth left at 0 (auto) come from the autotuner, which runs on first use
 Variant pick_variant(const pg_opts* o)
 {
     Engine& E = engine();
-    Variant v{PG_SLIDER_KOGGE_STONE, 256};
+    Variant v;
     int sl = o ? o->slider : PG_SLIDER_AUTO;
     if (sl == PG_SLIDER_AUTO) sl = E.default_slider;
-    if (sl == PG_SLIDER_AUTO) sl = PG_SLIDER_KOGGE_STONE;
-    v.slider = sl;
+    const bool auto_all = sl == PG_SLIDER_AUTO && !(o && o->block_size) && !(o && o->leaf_plies);
+    if (auto_all && !E.tuned) autotune_locked();
+    if (auto_all && E.tuned) {
+        v.per_depth = true;
+        v.leaf_plies = E.tuned_leaf_plies;
+        v.slider = PG_SLIDER_KOGGE_STONE;  // expansions; leaves use the table
+        return v;
+    }
+    v.slider = sl == PG_SLIDER_AUTO ? PG_SLIDER_KOGGE_STONE : sl;
     if (o && (o->block_size == 128 || o->block_size == 256 || o->block_size == 512)) v.T = o->block_size;
+    if (o && (o->leaf_plies == 1 || o->leaf_plies == 2)) v.leaf_plies = o->leaf_plies;
     return v;
 }
 
@@ -317,13 +432,9 @@ static int end_call(const pg_opts* o)
 // perft of n roots; each root's count is added to acc[group] (group =
 // groups[i], or i when groups is null).  acc is zeroed first when zero_acc.
 int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc, bool zero_acc,
-               int slider, int block)
+               const Variant& v)
 {
     Engine& E = engine();
-    pg_opts o{};
-    o.slider = slider;
-    o.block_size = block;
-    const Variant v = pick_variant(&o);
     PG_TRY(ensure_level(0, n));
     if (zero_acc) PG_CUDA(cudaMemsetAsync(acc, 0, (u64)n * sizeof(u64), E.stream));
     u32* ctr = (u32*)(E.host_scratch + 64);  // pinned, 4 words
@@ -356,7 +467,7 @@ int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_gro
 static int perft_batch_device_locked(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out,
                                      const pg_opts* o)
 {
-    return perft_core(d_pos, d_depths, nullptr, n, d_out, true, o ? o->slider : 0, o ? o->block_size : 0);
+    return perft_core(d_pos, d_depths, nullptr, n, d_out, true, pick_variant(o));
 }
 
 // The positions `plies` plies below root (all of them, in generateMoves
@@ -623,6 +734,28 @@ int pg_random_playouts(uint64_t seed, uint32_t n, int min_plies, int max_plies, 
     PG_CUDA(cudaMemcpyAsync(out, d, (u64)n * 48, cudaMemcpyDeviceToHost, E.stream));
     if (depths) PG_CUDA(cudaMemcpyAsync(depths, dd, n, cudaMemcpyDeviceToHost, E.stream));
     return end_call(nullptr);
+}
+
+int pg_autotune(pg_tuning* out)
+{
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    if (!E.tuned) {
+        E.ticket_next = 0;
+        PG_CUDA(cudaMemsetAsync(E.tickets, 0, MAX_TICKETS * sizeof(u32), E.stream));
+        PG_TRY(autotune_locked());
+    }
+    if (out) {
+        out->leaf_plies = E.tuned_leaf_plies;
+        for (int d = 0; d < 16; d++) {
+            out->slider[d] = E.tuned_slider[d];
+            out->block_size[d] = E.tuned_T[d];
+            out->leaves_per_s[d] = E.tuned_rate[d];
+        }
+        out->seconds = E.tune_seconds;
+    }
+    return PG_OK;
 }
 
 int pg_tt_clear(void)

@@ -79,6 +79,13 @@ struct Engine {
     u64* host_scratch = nullptr;   // pinned small scratch
     // statistics of the current call
     pg_stats st{};
+    // autotuner result: best leaf variant per root depth, switch depth
+    bool tuned = false;
+    int tuned_leaf_plies = 2;
+    int tuned_slider[16] = {};
+    int tuned_T[16] = {};
+    double tuned_rate[16] = {};
+    double tune_seconds = 0;
 };
 
 Engine& engine();
@@ -86,8 +93,10 @@ void set_error(const char* fmt, ...);
 
 // engine internals shared by the translation units (call with engine().mu held)
 struct Variant {
-    int slider;  // pg_slider (never AUTO here)
-    int T;       // CTA size of the block-queue kernels
+    int slider = PG_SLIDER_KOGGE_STONE;  // pg_slider (never AUTO here)
+    int T = 256;                         // CTA size of the block-queue kernels
+    int leaf_plies = 2;                  // plies finished inside one CTA (switch depth)
+    bool per_depth = false;              // take the leaf kernel's slider/T from the tuning table
 };
 Variant pick_variant(const pg_opts* o);
 u32* next_ticket();
@@ -100,7 +109,7 @@ u64 level_cap_max();
 int ensure_level(int L, u64 need);
 int ensure_stage(u64 bytes);
 int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc, bool zero_acc,
-               int slider, int block);
+               const Variant& v);
 int expand_frontier(const Pos& root, int plies, Pos* out, u32 cap, u32* n_out);
 
 }  // namespace pg

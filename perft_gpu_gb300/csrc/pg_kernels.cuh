@@ -215,12 +215,12 @@ __global__ void k_playouts(Pos start, u64 seed, u32 n, int min_plies, int max_pl
 // ---------------------------------------------------------------------------
 
 template <int S, class SL>
-__global__ void k_count_level(LevelView lv, u32 start, u32 n, u32* __restrict__ cnt)
+__global__ void k_count_level(LevelView lv, u32 start, u32 n, u32* __restrict__ cnt, u32 min_rem)
 {
     stage_tables<SL>();
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const u32 rem = lv.rem[start + i];
-        cnt[i] = (rem >= 3 && rem < REM_DEAD) ? count_moves<S, SL>(load_board(lv, start + i)) : 0u;
+        cnt[i] = (rem >= min_rem && rem < REM_DEAD) ? count_moves<S, SL>(load_board(lv, start + i)) : 0u;
     }
 }
 
@@ -239,7 +239,8 @@ template <int T> constexpr int min_blocks() { return (PG_LEAF_MIN_WARPS * 32 + T
 
 // the last plies of every node with remaining depth <= 2, inside one CTA
 template <int S, class SL, int T, int QCAP>
-__global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket)
+__global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
+                                                            u32 max_rem)
 {
     extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     stage_tables<SL>();
@@ -263,7 +264,7 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
             b = load_board(lv, start + i);
             grp = lv.grp[start + i];
             const int rem = lv.rem[start + i];
-            if (rem == 2) c = count_moves<S, SL>(b);
+            if (rem == 2 && max_rem >= 2) c = count_moves<S, SL>(b);
             else if (rem == 1) ga.add(acc, grp, count_moves<S, SL>(b));
             else if (rem == 0) ga.add(acc, grp, 1);
         }

@@ -166,7 +166,7 @@ void launch_leaf_na(const LevelView& lv, u32 start, u32 n, u64* out, u32* ticket
     constexpr int Q = NA_T * 32;
     using L = BlockSmem<SlKS, NA_T, Q>;
     auto fn = k_leaf<S, SlKS, NA_T, Q>;
-    fn<<<grid_of((const void*)fn, NA_T, L::bytes, n, sms), NA_T, L::bytes, st>>>(lv, start, n, out, ticket);
+    fn<<<grid_of((const void*)fn, NA_T, L::bytes, n, sms), NA_T, L::bytes, st>>>(lv, start, n, out, ticket, 2u);
 }
 
 template <int S>
@@ -184,7 +184,7 @@ template <int S>
 void launch_count_na(const LevelView& lv, u32 start, u32 n, u32* cnt, cudaStream_t st, int sms)
 {
     auto fn = k_count_level<S, SlKS>;
-    fn<<<grid_of((const void*)fn, 256, 0, n, sms), 256, 0, st>>>(lv, start, n, cnt);
+    fn<<<grid_of((const void*)fn, 256, 0, n, sms), 256, 0, st>>>(lv, start, n, cnt, 3u);
 }
 
 }  // namespace

@@ -14,11 +14,11 @@ struct SliderOps {
     int slider;  // pg_slider
     cudaError_t (*upload)(const HostTables& t);
     cudaError_t (*leaf)(int side, int T, const LevelView& lv, u32 start, u32 n, u64* acc, u32* ticket,
-                        cudaStream_t st, int num_sms);
+                        u32 max_rem, cudaStream_t st, int num_sms);
     cudaError_t (*expand)(int side, int T, const LevelView& in, u32 start, u32 a, u32 b, const u64* offs,
                           const LevelView& out, u32* ticket, cudaStream_t st, int num_sms);
-    cudaError_t (*count_level)(int side, const LevelView& lv, u32 start, u32 n, u32* cnt, cudaStream_t st,
-                               int num_sms);
+    cudaError_t (*count_level)(int side, const LevelView& lv, u32 start, u32 n, u32* cnt, u32 min_rem,
+                               cudaStream_t st, int num_sms);
     cudaError_t (*count_batch)(const Pos* in, u32 n, u32* out, cudaStream_t st);
     cudaError_t (*gen_moves_batch)(const Pos* in, u32 n, u16* out, u32* nout, cudaStream_t st);
     cudaError_t (*gen_boards_batch)(const Pos* in, u32 n, Pos* out, u32* nout, cudaStream_t st);

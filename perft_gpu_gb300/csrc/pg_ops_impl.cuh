@@ -46,7 +46,8 @@ template <class K> cudaError_t set_smem(K fn, int bytes)
 }
 
 template <int S, class SL, int T>
-cudaError_t leaf_t(const LevelView& lv, u32 start, u32 n, u64* acc, u32* ticket, cudaStream_t st, int sms)
+cudaError_t leaf_t(const LevelView& lv, u32 start, u32 n, u64* acc, u32* ticket, u32 max_rem, cudaStream_t st,
+                   int sms)
 {
     constexpr int Q = QcapFor<SL, T>::value;
     using L = BlockSmem<SL, T, Q>;
@@ -54,7 +55,7 @@ cudaError_t leaf_t(const LevelView& lv, u32 start, u32 n, u64* acc, u32* ticket,
     static cudaError_t attr = set_smem(fn, L::bytes);
     if (attr) return attr;
     const int grid = occupancy_grid((const void*)fn, T, L::bytes, n, sms);
-    fn<<<grid, T, L::bytes, st>>>(lv, start, n, acc, ticket);
+    fn<<<grid, T, L::bytes, st>>>(lv, start, n, acc, ticket, max_rem);
     return cudaGetLastError();
 }
 
@@ -73,12 +74,17 @@ cudaError_t expand_t(const LevelView& in, u32 start, u32 a, u32 b, const u64* of
 }
 
 template <class SL>
-cudaError_t leaf_any(int side, int T, const LevelView& lv, u32 start, u32 n, u64* acc, u32* ticket, cudaStream_t st,
-                     int sms)
+cudaError_t leaf_any(int side, int T, const LevelView& lv, u32 start, u32 n, u64* acc, u32* ticket, u32 max_rem,
+                     cudaStream_t st, int sms)
 {
-    if (T == 128) return side ? leaf_t<1, SL, 128>(lv, start, n, acc, ticket, st, sms) : leaf_t<0, SL, 128>(lv, start, n, acc, ticket, st, sms);
-    if (T == 512) return side ? leaf_t<1, SL, 512>(lv, start, n, acc, ticket, st, sms) : leaf_t<0, SL, 512>(lv, start, n, acc, ticket, st, sms);
-    return side ? leaf_t<1, SL, 256>(lv, start, n, acc, ticket, st, sms) : leaf_t<0, SL, 256>(lv, start, n, acc, ticket, st, sms);
+    if (T == 128)
+        return side ? leaf_t<1, SL, 128>(lv, start, n, acc, ticket, max_rem, st, sms)
+                    : leaf_t<0, SL, 128>(lv, start, n, acc, ticket, max_rem, st, sms);
+    if (T == 512)
+        return side ? leaf_t<1, SL, 512>(lv, start, n, acc, ticket, max_rem, st, sms)
+                    : leaf_t<0, SL, 512>(lv, start, n, acc, ticket, max_rem, st, sms);
+    return side ? leaf_t<1, SL, 256>(lv, start, n, acc, ticket, max_rem, st, sms)
+                : leaf_t<0, SL, 256>(lv, start, n, acc, ticket, max_rem, st, sms);
 }
 
 template <class SL>
@@ -91,21 +97,23 @@ cudaError_t expand_any(int side, int T, const LevelView& in, u32 start, u32 a, u
 }
 
 template <int S, class SL>
-cudaError_t count_level_t(const LevelView& lv, u32 start, u32 n, u32* cnt, cudaStream_t st, int sms)
+cudaError_t count_level_t(const LevelView& lv, u32 start, u32 n, u32* cnt, u32 min_rem, cudaStream_t st, int sms)
 {
     auto fn = k_count_level<S, SL>;
     constexpr int smem = table_smem_bytes<SL>();
     static cudaError_t attr = set_smem(fn, smem);
     if (attr) return attr;
     const int grid = occupancy_grid((const void*)fn, 256, smem, n, sms);
-    fn<<<grid, 256, smem, st>>>(lv, start, n, cnt);
+    fn<<<grid, 256, smem, st>>>(lv, start, n, cnt, min_rem);
     return cudaGetLastError();
 }
 
 template <class SL>
-cudaError_t count_level_any(int side, const LevelView& lv, u32 start, u32 n, u32* cnt, cudaStream_t st, int sms)
+cudaError_t count_level_any(int side, const LevelView& lv, u32 start, u32 n, u32* cnt, u32 min_rem, cudaStream_t st,
+                            int sms)
 {
-    return side ? count_level_t<1, SL>(lv, start, n, cnt, st, sms) : count_level_t<0, SL>(lv, start, n, cnt, st, sms);
+    return side ? count_level_t<1, SL>(lv, start, n, cnt, min_rem, st, sms)
+                : count_level_t<0, SL>(lv, start, n, cnt, min_rem, st, sms);
 }
 
 inline int small_grid(u32 n, int T) { return (int)std::max<u32>(1, std::min<u32>((n + T - 1) / T, 8192)); }

@@ -259,7 +259,9 @@ int run_wave(Server& S, std::unique_lock<std::mutex>& lk)
     E.ticket_next = 0;
     cudaMemsetAsync(E.tickets, 0, MAX_TICKETS * sizeof(u32), E.stream);
     cudaMemsetAsync(E.err, 0, sizeof(u32), E.stream);
-    int st = perft_core(S.wave_pos, S.wave_dep, S.wave_grp, total, S.acc, false, S.slider, 0);
+    pg_opts o{};
+    o.slider = S.slider;
+    int st = perft_core(S.wave_pos, S.wave_dep, S.wave_grp, total, S.acc, false, pick_variant(&o));
     if (st == PG_OK) {
         if (cudaMemcpyAsync(S.acc_host, S.acc, S.max_inflight * sizeof(u64), cudaMemcpyDeviceToHost, E.stream) !=
                 cudaSuccess ||

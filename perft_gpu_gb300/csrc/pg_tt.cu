@@ -391,7 +391,8 @@ int tt_perft_batch_device(const Pos* d_pos, const unsigned char* d_depths, u32 n
     if (!g_tt.keys_ready) TT_TRY(tt_upload_keys());
     u64 bytes = (o && o->tt_bytes) ? o->tt_bytes : std::min<u64>(32ull << 30, E.budget / 4);
     TT_TRY(ensure_tables(bytes));
-    const Variant v = pick_variant(o);
+    Variant v = pick_variant(o);
+    v.leaf_plies = 2;  // the TT driver finishes the last two plies in the leaf kernel
     TT_TRY(ensure_level(0, n));
     TT_TRY(ensure_level_tt(0, n));
     if (g_tt.root_cap < n) {

@@ -110,3 +110,29 @@ def test_batch_equals_sum_of_singles(pg):
     mixed = pg.perft_batch(boards, depths)
     alone = [pg.perft(pg.board_of(boards[i]), int(depths[i])) for i in range(len(idx))]
     assert [int(x) for x in mixed] == alone
+
+
+def test_switch_depth_one_ply_leaf(pg):
+    """Breadth-first down to the leaf-parents, count-only leaf: same counts."""
+    for item in golden_json("fens.json")[:4]:
+        b = pg.board_from_fen(item["fen"])
+        for d in ("3", "4", "5"):
+            assert pg.perft(b, int(d), leaf_plies=1, slider="ks") == item["perft"][d]
+    g = golden_npz("config3.npz")
+    idx = np.arange(0, 4096, 13)
+    boards = g["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    depths = np.minimum(g["depths"][idx], 5)
+    assert np.array_equal(pg.perft_batch(boards, depths, leaf_plies=1, slider="fancy"),
+                          pg.perft_batch(boards, depths, slider="ks"))
+
+
+def test_autotuner_choices_and_auto_counts(pg):
+    t = pg.autotune()
+    assert t["leaf_plies"] in (1, 2) and t["seconds"] > 0
+    for d, c in t["per_depth"].items():
+        assert c["slider"] in ("ks", "fancy", "byte") and c["block_size"] in (128, 256, 512)
+        assert c["calibration_leaves_per_s"] > 0
+    g = golden_npz("config3.npz")
+    idx = np.arange(0, 4096, 29)
+    boards = g["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    assert np.array_equal(pg.perft_batch(boards, g["depths"][idx]), g["totals"][idx])
