@@ -348,6 +348,27 @@ def run_ours(args):
     elapsed_max = max_over_ranks(dist, elapsed)
     value = leaves_per_step * args.steps * world / elapsed_max
 
+    # the same steps replayed from a captured CUDA graph (first call captures)
+    def step_graph():
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        pg.perft_batch_device(d_boards.data_ptr(), d_depths.data_ptr(), n, d_out.data_ptr(), slider=slider,
+                              graph=True)
+    step_graph()
+    assert int(d_out.cpu().numpy().view(np.uint64).sum()) == leaves_per_step
+    barrier(dist)
+    torch.cuda.synchronize()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(args.steps):
+        step_graph()
+    g1.record(stream)
+    torch.cuda.synchronize()
+    graph_el = max_over_ranks(dist, g0.elapsed_time(g1) / 1e3)
+    graph_value = leaves_per_step * args.steps * world / graph_el
+    assert int(d_out.cpu().numpy().view(np.uint64).sum()) == leaves_per_step
+
     # end to end through the public API with host buffers
     pin_b = torch.from_numpy(boards.view(np.uint8).copy()).pin_memory()
     pin_d = torch.from_numpy(depths.copy()).pin_memory()
@@ -437,6 +458,10 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "leaf nodes/s",
                     "h2d_bytes_per_step": n * 48 + n, "d2h_bytes_per_step": n * 8},
             "gpu_launches": launches,
+            "graph_replay": {"value": graph_value, "unit": "leaf nodes/s",
+                             "ms_per_step": 1e3 * graph_el / args.steps,
+                             "note": "same steps replayed from one captured CUDA graph per step"},
+            "autotune": pg.autotune(),
             "plain": plain,
             "batched_vs_plain": (value / plain["value"]) if plain else None,
             "roofline": {"bound": "hbm", "kernel": "k_leaf", "achieved": achieved, "peak": peak,

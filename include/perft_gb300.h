@@ -75,6 +75,8 @@ typedef struct pg_stats {
     uint64_t leaf_kernel_launches;
     double leaf_kernel_ms;       /* CUDA-event time of the leaf (2-ply) kernel launches */
     uint64_t leaf_parent_nodes;  /* nodes handed to the leaf kernel (each 2 plies above a leaf) */
+    uint64_t graph_captures;     /* 1 when this call captured its launch sequence into a graph */
+    uint64_t graph_replays;      /* 1 when this call replayed a captured graph */
 } pg_stats;
 
 typedef struct pg_opts {

@@ -95,7 +95,8 @@ class PgStats(ctypes.Structure):
                 ("launches", ctypes.c_uint64), ("peak_level_bytes", ctypes.c_uint64),
                 ("tt_probes", ctypes.c_uint64), ("tt_hits", ctypes.c_uint64),
                 ("tt_stores", ctypes.c_uint64), ("leaf_kernel_launches", ctypes.c_uint64),
-                ("leaf_kernel_ms", ctypes.c_double), ("leaf_parent_nodes", ctypes.c_uint64)]
+                ("leaf_kernel_ms", ctypes.c_double), ("leaf_parent_nodes", ctypes.c_uint64),
+                ("graph_captures", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -214,34 +214,54 @@ static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int mi
     LevelBuf& lb = E.lv[L];
     E.st.peak_level_bytes = std::max<uint64_t>(E.st.peak_level_bytes, (uint64_t)n * 48);
     const int lp = v.leaf_plies;
+    const bool capturing = E.plan_mode == PLAN_REPLAY;
     if (minrem <= lp) {
-        cudaEventRecord(E.lev0, E.stream);
+        if (!capturing) cudaEventRecord(E.lev0, E.stream);
         PG_TRY(launch_leaf(leaf_variant(v, L), side, lb.v, start, n, acc));
-        cudaEventRecord(E.lev1, E.stream);
-        float ms = 0;
-        PG_CUDA(cudaEventSynchronize(E.lev1));
-        cudaEventElapsedTime(&ms, E.lev0, E.lev1);
-        E.st.leaf_kernel_ms += ms;
+        if (!capturing) {
+            cudaEventRecord(E.lev1, E.stream);
+            float ms = 0;
+            PG_CUDA(cudaEventSynchronize(E.lev1));
+            cudaEventElapsedTime(&ms, E.lev0, E.lev1);
+            E.st.leaf_kernel_ms += ms;
+        }
     }
     if (maxrem <= lp) return PG_OK;
     PG_TRY(launch_count(v, side, lb.v, start, n, lb.cnt));
     PG_TRY(launch_scan(lb.cnt, n, lb.offs));
-    const u64 cap_next = level_cap_max();
-    k_plan<<<1, 32, 0, E.stream>>>(lb.offs, n, cap_next, E.plan_dev, E.err);
-    PG_CUDA(cudaGetLastError());
-    E.st.launches++;
-    PG_CUDA(cudaMemcpyAsync(E.plan_host, E.plan_dev, sizeof(PlanOut), cudaMemcpyDeviceToHost, E.stream));
-    PG_CUDA(cudaStreamSynchronize(E.stream));
-    u32 errv = 0;
-    PG_CUDA(cudaMemcpy(&errv, E.err, sizeof(u32), cudaMemcpyDeviceToHost));
-    if (errv) {
-        set_error("device error flags 0x%x while planning level %d", errv, L);
-        return PG_ERR_DEVICE_TIMEOUT;
+    std::vector<u32> bnd;
+    std::vector<u64> boff;
+    if (capturing) {
+        // the chunk plan recorded by the previous run of the same inputs
+        if (E.rec_next >= E.rec_bnd.size()) {
+            set_error("recorded launch plan does not match the inputs");
+            return PG_ERR_INVALID_ARGUMENT;
+        }
+        bnd = E.rec_bnd[E.rec_next];
+        boff = E.rec_off[E.rec_next];
+        E.rec_next++;
+    } else {
+        const u64 cap_next = level_cap_max();
+        k_plan<<<1, 32, 0, E.stream>>>(lb.offs, n, cap_next, E.plan_dev, E.err);
+        PG_CUDA(cudaGetLastError());
+        E.st.launches++;
+        PG_CUDA(cudaMemcpyAsync(E.plan_host, E.plan_dev, sizeof(PlanOut), cudaMemcpyDeviceToHost, E.stream));
+        PG_CUDA(cudaStreamSynchronize(E.stream));
+        u32 errv = 0;
+        PG_CUDA(cudaMemcpy(&errv, E.err, sizeof(u32), cudaMemcpyDeviceToHost));
+        if (errv) {
+            set_error("device error flags 0x%x while planning level %d", errv, L);
+            return PG_ERR_DEVICE_TIMEOUT;
+        }
+        const PlanOut& plan = *E.plan_host;  // copied out: deeper levels reuse the pinned buffer
+        bnd.assign(plan.bnd, plan.bnd + plan.nchunks + 1);
+        boff.assign(plan.coff, plan.coff + plan.nchunks + 1);
+        if (E.plan_mode == PLAN_RECORD) {
+            E.rec_bnd.push_back(bnd);
+            E.rec_off.push_back(boff);
+        }
     }
-    const PlanOut plan = *E.plan_host;  // copy: deeper levels reuse the pinned buffer
-    std::vector<u32> bnd(plan.bnd, plan.bnd + plan.nchunks + 1);
-    if (plan.total == 0) return PG_OK;
-    std::vector<u64> boff(plan.coff, plan.coff + plan.nchunks + 1);
+    if (boff.back() == boff.front()) return PG_OK;
     const int cminrem = std::max(minrem, lp + 1) - 1, cmaxrem = maxrem - 1;
     for (size_t k = 0; k + 1 < bnd.size(); k++) {
         const u32 a = bnd[k], b = bnd[k + 1];
@@ -435,31 +455,124 @@ int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_gro
                const Variant& v)
 {
     Engine& E = engine();
+    const bool capturing = E.plan_mode == PLAN_REPLAY;
     PG_TRY(ensure_level(0, n));
     if (zero_acc) PG_CUDA(cudaMemsetAsync(acc, 0, (u64)n * sizeof(u64), E.stream));
     u32* ctr = (u32*)(E.host_scratch + 64);  // pinned, 4 words
-    u32* dctr = E.tickets + MAX_TICKETS - 4;
-    const u32 init[4] = {0, 0, 0xFFFFFFFFu, 0};
-    PG_CUDA(cudaMemcpyAsync(dctr, init, sizeof(init), cudaMemcpyHostToDevice, E.stream));
+    u32* dctr = E.tickets + MAX_TICKETS - 4;  // white count, black count, min depth, max depth
+    PG_CUDA(cudaMemsetAsync(dctr, 0, 4 * sizeof(u32), E.stream));
+    PG_CUDA(cudaMemsetAsync(dctr + 2, 0xFF, sizeof(u32), E.stream));
     k_partition_roots<<<std::max<u32>(1, std::min<u32>((n + 255) / 256, 4096)), 256, 0, E.stream>>>(
         d_pos, d_depths, n, E.lv[0].v, dctr, d_groups);
     PG_CUDA(cudaGetLastError());
     E.st.launches++;
-    PG_CUDA(cudaMemcpyAsync(ctr, dctr, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
-    PG_CUDA(cudaStreamSynchronize(E.stream));
-    const u32 nw = ctr[0], mind = ctr[2], maxd = ctr[3];
+    u32 nw, mind, maxd;
+    if (capturing) {
+        nw = E.rec_part[0];
+        mind = E.rec_part[2];
+        maxd = E.rec_part[3];
+    } else {
+        PG_CUDA(cudaMemcpyAsync(ctr, dctr, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+        PG_CUDA(cudaStreamSynchronize(E.stream));
+        nw = ctr[0];
+        mind = ctr[2];
+        maxd = ctr[3];
+        if (E.plan_mode == PLAN_RECORD) memcpy(E.rec_part, ctr, sizeof(E.rec_part));
+    }
     if (maxd > 15) {
         set_error("depth %u out of range 0..15", maxd);
         return PG_ERR_INVALID_ARGUMENT;
     }
-    cudaEventRecord(E.ev0, E.stream);
+    if (!capturing) cudaEventRecord(E.ev0, E.stream);
     PG_TRY(run_range(v, 0, 0, nw, 0, (int)mind, (int)maxd, acc));
     PG_TRY(run_range(v, 0, nw, n - nw, 1, (int)mind, (int)maxd, acc));
-    cudaEventRecord(E.ev1, E.stream);
-    PG_CUDA(cudaEventSynchronize(E.ev1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, E.ev0, E.ev1);
-    E.st.device_ms = ms;
+    if (!capturing) {
+        cudaEventRecord(E.ev1, E.stream);
+        PG_CUDA(cudaEventSynchronize(E.ev1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+        E.st.device_ms = ms;
+    }
+    return PG_OK;
+}
+
+// Batch perft replayed from a captured CUDA graph.  The first call on a set
+// of inputs runs normally while recording its data-dependent launch plan
+// (root partition, chunk boundaries), then captures the same launch sequence
+// without any host synchronisation into a graph; later calls whose inputs
+// (pointers, size, and a device checksum of the contents) and variant are
+// unchanged launch that graph.
+static int perft_batch_graph_locked(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out,
+                                    const pg_opts* o)
+{
+    Engine& E = engine();
+    const Variant v = pick_variant(o);
+    PG_CUDA(cudaMemsetAsync(E.aux, 0, sizeof(u64), E.stream));
+    k_checksum<<<std::max<u32>(1, std::min<u32>((n + 255) / 256, 1024)), 256, 0, E.stream>>>(d_pos, d_depths, n,
+                                                                                           E.aux);
+    PG_CUDA(cudaGetLastError());
+    PG_CUDA(cudaMemcpyAsync(E.host_scratch + 128, E.aux, sizeof(u64), cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    const u64 sum = E.host_scratch[128];
+    GraphCache& g = E.graph;
+    const bool hit = g.exec && g.pos == d_pos && g.dep == d_depths && g.out == d_out && g.n == n && g.sum == sum &&
+                     g.slider == v.slider && g.T == v.T && g.leaf_plies == v.leaf_plies && g.per_depth == v.per_depth;
+    if (hit) {
+        cudaEventRecord(E.ev0, E.stream);
+        PG_CUDA(cudaGraphLaunch(g.exec, E.stream));
+        cudaEventRecord(E.ev1, E.stream);
+        PG_CUDA(cudaEventSynchronize(E.ev1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+        E.st.device_ms = ms;
+        E.st.launches = g.launches;
+        E.st.graph_replays = 1;
+        return PG_OK;
+    }
+    // record: a normal run computes this call's result and the launch plan
+    E.rec_bnd.clear();
+    E.rec_off.clear();
+    E.plan_mode = PLAN_RECORD;
+    int rc = perft_core(d_pos, d_depths, nullptr, n, d_out, true, v);
+    E.plan_mode = PLAN_NONE;
+    if (rc != PG_OK) return rc;
+    const pg_stats rec_stats = E.st;
+    // capture the same launches with the recorded plan
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = GraphCache{};
+    const u32 tickets_used = E.ticket_next;
+    E.ticket_next = 0;
+    E.rec_next = 0;
+    cudaGraph_t graph = nullptr;
+    PG_CUDA(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
+    E.plan_mode = PLAN_REPLAY;
+    cudaMemsetAsync(E.tickets, 0, (u64)tickets_used * sizeof(u32), E.stream);
+    cudaMemsetAsync(E.err, 0, sizeof(u32), E.stream);
+    rc = perft_core(d_pos, d_depths, nullptr, n, d_out, true, v);
+    E.plan_mode = PLAN_NONE;
+    const cudaError_t ce = cudaStreamEndCapture(E.stream, &graph);
+    E.st = rec_stats;
+    if (rc != PG_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    PG_CUDA(ce);
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    PG_CUDA(ie);
+    g.exec = exec;
+    g.pos = d_pos;
+    g.dep = d_depths;
+    g.out = d_out;
+    g.n = n;
+    g.sum = sum;
+    g.slider = v.slider;
+    g.T = v.T;
+    g.leaf_plies = v.leaf_plies;
+    g.per_depth = v.per_depth;
+    g.launches = rec_stats.launches;
+    E.st.graph_captures = 1;
     return PG_OK;
 }
 
@@ -591,6 +704,7 @@ int pg_init(const pg_config* cfg)
     PG_CUDA(cudaMalloc(&E.plan_dev, sizeof(PlanOut)));
     PG_CUDA(cudaMallocHost(&E.plan_host, sizeof(PlanOut)));
     PG_CUDA(cudaMallocHost(&E.host_scratch, 4096));
+    PG_CUDA(cudaMalloc(&E.aux, 256));
     PG_CUDA(cudaDeviceSynchronize());
     E.ready = true;
     return PG_OK;
@@ -614,6 +728,9 @@ int pg_shutdown(void)
     cudaFree(E.plan_dev);
     cudaFreeHost(E.plan_host);
     cudaFreeHost(E.host_scratch);
+    cudaFree(E.aux);
+    if (E.graph.exec) cudaGraphExecDestroy(E.graph.exec);
+    E.graph = GraphCache{};
     cudaEventDestroy(E.ev0);
     cudaEventDestroy(E.ev1);
     cudaEventDestroy(E.lev0);
@@ -777,6 +894,8 @@ int pg_perft_batch_device(const pg_board* d_pos, const uint8_t* d_depths, uint32
     PG_TRY(begin_call(opts));
     if (opts && opts->use_tt) {
         PG_TRY(tt_perft_batch_device((const Pos*)d_pos, d_depths, n, (u64*)d_out, opts));
+    } else if (opts && opts->graph) {
+        PG_TRY(perft_batch_graph_locked((const Pos*)d_pos, d_depths, n, (u64*)d_out, opts));
     } else {
         PG_TRY(perft_batch_device_locked((const Pos*)d_pos, d_depths, n, (u64*)d_out, opts));
     }
@@ -805,6 +924,8 @@ int pg_perft_batch(const pg_board* pos, const uint8_t* depths, uint32_t n, uint6
     PG_CUDA(cudaMemcpyAsync(d_dep, depths, n, cudaMemcpyHostToDevice, E.stream));
     if (opts && opts->use_tt) {
         PG_TRY(tt_perft_batch_device(d_pos, d_dep, n, d_out, opts));
+    } else if (opts && opts->graph) {
+        PG_TRY(perft_batch_graph_locked(d_pos, d_dep, n, d_out, opts));
     } else {
         PG_TRY(perft_batch_device_locked(d_pos, d_dep, n, d_out, opts));
     }

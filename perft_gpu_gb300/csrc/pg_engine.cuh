@@ -52,6 +52,21 @@ struct PlanOut {
     u64 coff[MAX_CHUNKS + 1];  // offs[] at each boundary
 };
 
+enum PlanMode { PLAN_NONE = 0, PLAN_RECORD = 1, PLAN_REPLAY = 2 };
+
+// one captured batch (see perft_batch_graph_locked)
+struct GraphCache {
+    cudaGraphExec_t exec = nullptr;
+    const void* pos = nullptr;
+    const void* dep = nullptr;
+    const void* out = nullptr;
+    u32 n = 0;
+    u64 sum = 0;
+    int slider = 0, T = 0, leaf_plies = 0;
+    bool per_depth = false;
+    u64 launches = 0;
+};
+
 struct Engine {
     std::mutex mu;
     bool ready = false;
@@ -77,6 +92,14 @@ struct Engine {
     void* stage = nullptr;         // staging for host-array calls
     u64 stage_cap = 0;
     u64* host_scratch = nullptr;   // pinned small scratch
+    u64* aux = nullptr;            // small device scratch (input checksum)
+    // launch-plan recording for graph capture
+    int plan_mode = PLAN_NONE;
+    std::vector<std::vector<u32>> rec_bnd;
+    std::vector<std::vector<u64>> rec_off;
+    size_t rec_next = 0;
+    u32 rec_part[4] = {};
+    GraphCache graph;
     // statistics of the current call
     pg_stats st{};
     // autotuner result: best leaf variant per root depth, switch depth

@@ -156,6 +156,26 @@ static __global__ void k_plan(const u64* __restrict__ offs, u32 n, u64 cap, Plan
     plan->total = offs[n];
 }
 
+// order-sensitive 64-bit checksum of a batch (boards and depths)
+static __global__ void k_checksum(const Pos* __restrict__ pos, const unsigned char* __restrict__ dep, u32 n, u64* out)
+{
+    u64 h = 0;
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const Pos b = pos[i];
+        u64 x = (u64)i * 0x9E3779B97F4A7C15ull + dep[i];
+        const u64 w[6] = {b.w, b.p, b.n, b.bq, b.rq, b.k};
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            x ^= w[k] + 0x632BE59BD9B4E019ull * (k + 1);
+            x *= 0xD6E8FEB86659FD93ull;
+            x ^= x >> 32;
+        }
+        h ^= x;
+    }
+    for (int o = 16; o; o >>= 1) h ^= __shfl_xor_sync(0xFFFFFFFFu, h, o);
+    if ((threadIdx.x & 31) == 0 && h) atomicXor(out, h);
+}
+
 // level nodes [0, n) of one level buffer into an array of boards
 static __global__ void k_level_to_boards(LevelView lv, u32 n, Pos* __restrict__ out)
 {

@@ -136,3 +136,24 @@ def test_autotuner_choices_and_auto_counts(pg):
     idx = np.arange(0, 4096, 29)
     boards = g["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
     assert np.array_equal(pg.perft_batch(boards, g["depths"][idx]), g["totals"][idx])
+
+
+def test_graph_capture_and_replay(pg):
+    """First call records its plan and captures a graph; repeats replay it;
+    new contents at the same pointers are detected and recaptured."""
+    g = golden_npz("config3.npz")
+    idx = np.arange(0, 4096, 11)
+    boards = g["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    depths = g["depths"][idx].copy()
+    seen = []
+    for k in range(3):
+        st = pg.PgStats()
+        out = pg.perft_batch(boards, depths, graph=True, stats=st)
+        assert np.array_equal(out, g["totals"][idx])
+        seen.append((st.graph_captures, st.graph_replays))
+    assert seen[0] == (1, 0) and seen[1] == (0, 1) and seen[2] == (0, 1)
+    other = np.arange(1, 4096, 11)[:len(idx)]
+    b2 = g["boards"][other].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    st = pg.PgStats()
+    out2 = pg.perft_batch(b2, g["depths"][other], graph=True, stats=st)
+    assert np.array_equal(out2, g["totals"][other]) and st.graph_captures == 1
