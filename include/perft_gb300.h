@@ -169,6 +169,25 @@ int pg_autotune(pg_tuning *out);
  * depend on what earlier calls stored).  No counterpart in the reference. */
 int pg_tt_clear(void);
 
+/* Divided perft at deep roots: perft_bb_cpu_launcher (launcher.h:1181-1389)
+ * with its complete transposition table (launcher.h:598-680).  The positions
+ * split_plies below each root move are made on the GPU and merged across all
+ * root moves in a host table keyed by the full board, so each distinct one is
+ * counted once; moves/counts as pg_perft_divide (generateMoves order).
+ * stats->tt_probes / tt_hits count the host table's lookups / repeats. */
+int pg_perft_split(const pg_board *pos, int depth, int split_plies, pg_move *moves, uint64_t *counts,
+                   uint32_t *n, const pg_opts *opts);
+
+/* Failure-detection self tests; neither faults nor hangs the GPU.
+ * PG_SELFTEST_BOUNDED_WAIT launches a scan tile whose predecessor never
+ * publishes: its poll gives up after the limit and the call returns
+ * PG_ERR_DEVICE_TIMEOUT, with the context still usable.
+ * PG_SELFTEST_FAIL_NEXT_ALLOC makes the next level allocation fail on the
+ * host, so the following call returns PG_ERR_OUT_OF_MEMORY and the one after
+ * it works.  No counterpart in the reference. */
+enum { PG_SELFTEST_BOUNDED_WAIT = 1, PG_SELFTEST_FAIL_NEXT_ALLOC = 2 };
+int pg_selftest(int which);
+
 /* ---- inputs ---- */
 /* Seeded random legal playouts from the initial position, generated on the
  * GPU.  Position i is the first accepted attempt a = 0, 1, ... of:

@@ -159,6 +159,8 @@ _SIGNATURES = {
     "pg_server_stop": [],
     "pg_tt_clear": [],
     "pg_autotune": [ctypes.POINTER(PgTuning)],
+    "pg_perft_split": [_BP, ctypes.c_int, ctypes.c_int, _U16P, _U64P, _U32P, _OP],
+    "pg_selftest": [ctypes.c_int],
 }
 
 _lib = None
@@ -281,6 +283,25 @@ def perft_divide(pos: HexaBitBoardPosition, depth: int, **kw) -> list[tuple[int,
     _check(load_library().pg_perft_divide(ctypes.byref(pos), depth, mv, cnt, ctypes.byref(n),
                                           ctypes.byref(o)))
     return [(mv[i], cnt[i]) for i in range(n.value)]
+
+
+def perft_split(pos: HexaBitBoardPosition, depth: int, split_plies: int = 3, **kw) -> list[tuple[int, int]]:
+    """Divided perft at deep roots with the host-side complete TT."""
+    mv = (ctypes.c_uint16 * 256)()
+    cnt = (ctypes.c_uint64 * 256)()
+    n = ctypes.c_uint32()
+    o = _opts(**kw)
+    _check(load_library().pg_perft_split(ctypes.byref(pos), depth, split_plies, mv, cnt, ctypes.byref(n),
+                                         ctypes.byref(o)))
+    return [(mv[i], cnt[i]) for i in range(n.value)]
+
+
+SELFTEST_BOUNDED_WAIT, SELFTEST_FAIL_NEXT_ALLOC = 1, 2
+
+
+def selftest(which: int) -> int:
+    """Returns the status code of a failure-detection self test."""
+    return load_library().pg_selftest(which)
 
 
 def perft_batch(boards: np.ndarray, depths: Iterable[int] | np.ndarray, **kw) -> np.ndarray:

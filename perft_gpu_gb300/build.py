@@ -18,6 +18,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libperft_gb300.so")
+CLI = os.path.join(HERE, "perft_gpu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
@@ -44,11 +45,12 @@ def _deps():
             deps.append(os.path.join(CSRC, f))
     deps.append(os.path.join(ROOT, "include", "perft_gb300.h"))
     deps.append(os.path.abspath(__file__))
+    deps.append(os.path.join(CSRC, "pg_cli.cpp"))
     return deps
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(d) <= t for d in _deps() if os.path.exists(d))
@@ -81,6 +83,13 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    # the command-line binary (perft.cu's argv) over the C ABI
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), os.path.join(CSRC, "pg_cli.cpp"),
+           "-o", CLI + ".tmp", "-L", HERE, "-lperft_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("perft_gpu link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

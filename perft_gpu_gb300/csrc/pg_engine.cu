@@ -16,6 +16,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "pg_engine.cuh"
@@ -160,7 +161,8 @@ int ensure_level(int L, u64 need)
     }
     const u64 bytes = cap * 48 + cap * 4 + cap + 16 + cap * 4 + (cap + 1) * 8 + 256;
     void* blk = nullptr;
-    cudaError_t e = cudaMalloc(&blk, bytes);
+    cudaError_t e = E.fail_next_alloc ? cudaErrorMemoryAllocation : cudaMalloc(&blk, bytes);
+    E.fail_next_alloc = false;
     if (e != cudaSuccess) {
         cudaGetLastError();
         set_error("level %d buffer of %llu nodes (%llu bytes) failed: %s", L, (unsigned long long)cap,
@@ -638,6 +640,159 @@ int expand_frontier(const Pos& root, int plies, Pos* out, u32 cap, u32* n_out)
     return PG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// divided perft at deep roots with a host-side complete transposition table
+// ---------------------------------------------------------------------------
+
+struct BoardKey {
+    u64 w[6];
+    bool operator==(const BoardKey& o) const { return !memcmp(w, o.w, sizeof(w)); }
+};
+struct BoardKeyHash {
+    size_t operator()(const BoardKey& k) const
+    {
+        u64 h = 0xCBF29CE484222325ull;
+        for (u64 x : k.w) {
+            h ^= x;
+            h *= 0x100000001B3ull;
+            h ^= h >> 29;
+        }
+        return (size_t)h;
+    }
+};
+
+// perft_bb_cpu_launcher (launcher.h:1181-1389) re-planned: every root move's
+// positions split_plies below the root are made on the GPU, merged across all
+// root moves in a host table keyed by the full board (the reference's
+// complete TT, launcher.h:598-680, without its hash collisions), and each
+// distinct position is counted once, in one batched engine call.
+int perft_split_locked(const Pos& root, int depth, int split, u16* moves, u64* counts, u32* nmoves,
+                       const pg_opts* o)
+{
+    Engine& E = engine();
+    if (split < 1) split = 1;
+    if (split > depth) split = depth;
+    // root moves and children (generateMoves order, makeMove children)
+    PG_TRY(ensure_stage(256 * 48 + 512 + 64));
+    Pos* d = (Pos*)E.stage;
+    u16* dm = (u16*)((unsigned char*)E.stage + 256 * 48);
+    u32* dn = (u32*)((unsigned char*)E.stage + 256 * 48 + 512);
+    PG_CUDA(cudaMemcpyAsync(d, &root, sizeof(Pos), cudaMemcpyHostToDevice, E.stream));
+    PG_CUDA(g_ops_ks.gen_moves_batch(d, 1, dm, dn, E.stream));
+    u32 n = 0;
+    PG_CUDA(cudaMemcpyAsync(moves, dm, 512, cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaMemcpyAsync(&n, dn, 4, cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    if (n > 256) {
+        set_error("more than 256 moves");
+        return PG_ERR_CAPACITY;
+    }
+    *nmoves = n;
+    if (!n) return PG_OK;
+    std::vector<Pos> kids(n, root);
+    PG_CUDA(cudaMemcpyAsync(d, kids.data(), n * sizeof(Pos), cudaMemcpyHostToDevice, E.stream));
+    PG_CUDA(g_ops_ks.make_batch(d, dm, n, E.stream));
+    PG_CUDA(cudaMemcpyAsync(kids.data(), d, n * sizeof(Pos), cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    const int rest = depth - split;  // depth left under each split position
+    std::unordered_map<BoardKey, u32, BoardKeyHash> table;
+    std::vector<Pos> uniq;
+    std::vector<std::vector<std::pair<u32, u64>>> uses(n);  // (unique index, multiplicity) per root move
+    const u32 cap = 1u << 24;
+    Pos* frontier = nullptr;
+    PG_CUDA(cudaMalloc(&frontier, (u64)cap * sizeof(Pos)));
+    std::vector<Pos> host;
+    int rc = PG_OK;
+    for (u32 i = 0; i < n && rc == PG_OK; i++) {
+        u32 m = 0;
+        if (split == 1) {
+            host.assign(1, kids[i]);
+            m = 1;
+        } else {
+            rc = expand_frontier(kids[i], split - 1, frontier, cap, &m);
+            if (rc != PG_OK) break;
+            host.resize(m);
+            if (m && cudaMemcpy(host.data(), frontier, (u64)m * sizeof(Pos), cudaMemcpyDeviceToHost) != cudaSuccess)
+                rc = PG_ERR_CUDA;
+        }
+        std::unordered_map<u32, u64> mult;
+        for (u32 k = 0; k < m; k++) {
+            BoardKey key;
+            memcpy(key.w, &host[k], sizeof(key.w));
+            key.w[1] &= ~(0x7Full << 56);  // the half-move clock does not change the count
+            auto it = table.find(key);
+            u32 u;
+            if (it == table.end()) {
+                u = (u32)uniq.size();
+                table.emplace(key, u);
+                uniq.push_back(host[k]);
+            } else {
+                u = it->second;
+            }
+            mult[u]++;
+        }
+        uses[i].assign(mult.begin(), mult.end());
+    }
+    cudaFree(frontier);
+    if (rc != PG_OK) return rc;
+    // count every distinct split position once
+    const u32 U = (u32)uniq.size();
+    std::vector<u64> res(U, 0);
+    if (U) {
+        PG_TRY(ensure_stage((u64)U * (48 + 1 + 8) + 64));
+        Pos* dp = (Pos*)E.stage;
+        unsigned char* dd = (unsigned char*)E.stage + (u64)U * 48;
+        u64* dout = (u64*)(((uintptr_t)(dd + U) + 15) & ~(uintptr_t)15);
+        PG_CUDA(cudaMemcpyAsync(dp, uniq.data(), (u64)U * 48, cudaMemcpyHostToDevice, E.stream));
+        PG_CUDA(cudaMemsetAsync(dd, rest, U, E.stream));
+        if (o && o->use_tt) PG_TRY(tt_perft_batch_device(dp, dd, U, dout, o));
+        else PG_TRY(perft_core(dp, dd, nullptr, U, dout, true, pick_variant(o)));
+        PG_CUDA(cudaMemcpyAsync(res.data(), dout, (u64)U * 8, cudaMemcpyDeviceToHost, E.stream));
+        PG_CUDA(cudaStreamSynchronize(E.stream));
+    }
+    u64 total_split = 0;
+    for (u32 i = 0; i < n; i++) {
+        u64 c = 0;
+        for (auto& [u, k] : uses[i]) {
+            c += k * res[u];
+            total_split += k;
+        }
+        counts[i] = c;
+    }
+    E.st.leaves = 0;
+    for (u32 i = 0; i < n; i++) E.st.leaves += counts[i];
+    E.st.tt_probes += total_split;        // split positions looked up in the host table
+    E.st.tt_hits += total_split - U;      // ... of which already present
+    return PG_OK;
+}
+
+// bounded-wait self test: a scan tile whose predecessor never publishes gives
+// up after its poll limit and raises the error bit (no fault, no hang)
+int selftest_bounded_wait()
+{
+    Engine& E = engine();
+    PG_TRY(ensure_stage(4096));
+    u32* cnt = (u32*)E.stage;
+    u64* offs = (u64*)((unsigned char*)E.stage + 1024);
+    u64* status = (u64*)((unsigned char*)E.stage + 2048);
+    u32* ticket = (u32*)((unsigned char*)E.stage + 3072);
+    PG_CUDA(cudaMemsetAsync(E.stage, 0, 4096, E.stream));
+    PG_CUDA(cudaMemsetAsync(E.err, 0, 4, E.stream));
+    const u32 one = 1;  // the only block takes tile 1 and waits on tile 0, which no block runs
+    PG_CUDA(cudaMemcpyAsync(ticket, &one, 4, cudaMemcpyHostToDevice, E.stream));
+    k_scan<<<1, SCAN_T, 0, E.stream>>>(cnt, 4096, offs, status, ticket, E.err);
+    PG_CUDA(cudaGetLastError());
+    u32 err = 0;
+    PG_CUDA(cudaMemcpyAsync(&err, E.err, 4, cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    if (err & ERR_SCAN_TIMEOUT) {
+        set_error("bounded wait gave up as designed (error bits 0x%x)", err);
+        return PG_ERR_DEVICE_TIMEOUT;
+    }
+    set_error("bounded wait did not report its timeout");
+    return PG_ERR_CUDA;
+}
+
 }  // namespace pg
 
 using namespace pg;
@@ -873,6 +1028,50 @@ int pg_autotune(pg_tuning* out)
         out->seconds = E.tune_seconds;
     }
     return PG_OK;
+}
+
+int pg_perft_split(const pg_board* pos, int depth, int split_plies, pg_move* moves, uint64_t* counts, uint32_t* n,
+                   const pg_opts* opts)
+{
+    if (!pos || !moves || !counts || !n || depth < 1 || depth > 15 || split_plies < 1) {
+        set_error("bad argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    if (!valid_board(*pos)) {
+        set_error("not a valid board");
+        return PG_ERR_INVALID_POSITION;
+    }
+    PG_TRY(begin_call(opts));
+    Pos root;
+    memcpy(&root, pos, sizeof(root));
+    PG_TRY(perft_split_locked(root, depth, split_plies, moves, (u64*)counts, n, opts));
+    PG_TRY(end_call(nullptr));
+    if (opts && opts->stats) *opts->stats = E.st;
+    return PG_OK;
+}
+
+int pg_selftest(int which)
+{
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    if (which == PG_SELFTEST_BOUNDED_WAIT) return selftest_bounded_wait();
+    if (which == PG_SELFTEST_FAIL_NEXT_ALLOC) {
+        E.fail_next_alloc = true;
+        // drop the level buffers so that the next call must allocate
+        cudaStreamSynchronize(E.stream);
+        for (auto& lb : E.lv) {
+            if (lb.block) cudaFree(lb.block);
+            lb = LevelBuf{};
+        }
+        E.level_bytes_total = 0;
+        return PG_OK;
+    }
+    set_error("unknown self test %d", which);
+    return PG_ERR_INVALID_ARGUMENT;
 }
 
 int pg_tt_clear(void)

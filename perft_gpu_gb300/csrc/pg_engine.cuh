@@ -109,6 +109,8 @@ struct Engine {
     int tuned_T[16] = {};
     double tuned_rate[16] = {};
     double tune_seconds = 0;
+    // host-side fault injection for tests: the next level allocation fails
+    bool fail_next_alloc = false;
 };
 
 Engine& engine();
