@@ -34,8 +34,8 @@ STATUS_NAMES = {0: "PG_OK", 1: "PG_ERR_NOT_INITIALIZED", 2: "PG_ERR_INVALID_ARGU
                 3: "PG_ERR_INVALID_POSITION", 4: "PG_ERR_CUDA", 5: "PG_ERR_OUT_OF_MEMORY",
                 6: "PG_ERR_DEVICE_TIMEOUT", 7: "PG_ERR_BUSY", 8: "PG_ERR_CAPACITY"}
 
-SLIDER_AUTO, SLIDER_KOGGE_STONE, SLIDER_FANCY, SLIDER_BYTE_SMEM = 0, 1, 2, 3
-SLIDERS = {"auto": 0, "ks": 1, "fancy": 2, "byte": 3}
+SLIDER_AUTO, SLIDER_KOGGE_STONE, SLIDER_FANCY, SLIDER_BYTE_SMEM, SLIDER_HYBRID = 0, 1, 2, 3, 4
+SLIDERS = {"auto": 0, "ks": 1, "fancy": 2, "byte": 3, "hybrid": 4}
 
 # CMove flags (chess.h:272-293)
 CM_FLAG_QUIET_MOVE, CM_FLAG_DOUBLE_PAWN_PUSH, CM_FLAG_KING_CASTLE, CM_FLAG_QUEEN_CASTLE = 0, 1, 2, 3

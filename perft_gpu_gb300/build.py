@@ -23,7 +23,7 @@ CLI = os.path.join(HERE, "perft_gpu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include")]
-CU_SOURCES = ["pg_engine.cu", "pg_sl_ks.cu", "pg_sl_fancy.cu", "pg_sl_byte.cu", "pg_tt.cu", "pg_noalloc.cu", "pg_server.cu"]
+CU_SOURCES = ["pg_engine.cu", "pg_sl_ks.cu", "pg_sl_fancy.cu", "pg_sl_byte.cu", "pg_sl_hybrid.cu", "pg_tt.cu", "pg_noalloc.cu", "pg_server.cu"]
 CPP_SOURCES = ["pg_host.cpp", "pg_tables.cpp"]
 
 

@@ -294,7 +294,9 @@ static int autotune_locked()
     };
     const Cal cals[] = {{3, 2048}, {4, 512}, {5, 64}, {6, 4}};
     const int cand[][2] = {{PG_SLIDER_KOGGE_STONE, 128}, {PG_SLIDER_KOGGE_STONE, 256}, {PG_SLIDER_KOGGE_STONE, 512},
-                           {PG_SLIDER_FANCY, 256},        {PG_SLIDER_FANCY, 512},        {PG_SLIDER_BYTE_SMEM, 512}};
+                           {PG_SLIDER_FANCY, 256},        {PG_SLIDER_FANCY, 512},        {PG_SLIDER_BYTE_SMEM, 512},
+                           {PG_SLIDER_HYBRID, 256},       {PG_SLIDER_HYBRID, 512}};
+    const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
     const u32 nmax = 2048;
     void* buf = nullptr;
     PG_CUDA(cudaMalloc(&buf, nmax * (48 + 1 + 8) + 256));
@@ -322,7 +324,7 @@ static int autotune_locked()
         }
         double best_ms = 1e30;
         int best = 1;
-        for (int k = 0; k < 6 && rc == PG_OK; k++) {
+        for (int k = 0; k < ncand && rc == PG_OK; k++) {
             Variant v;
             v.slider = cand[k][0];
             v.T = cand[k][1];
@@ -854,6 +856,7 @@ int pg_init(const pg_config* cfg)
     PG_CUDA(g_ops_ks.upload(*tabs));
     PG_CUDA(g_ops_fancy.upload(*tabs));
     PG_CUDA(g_ops_byte.upload(*tabs));
+    PG_CUDA(g_ops_hybrid.upload(*tabs));
     PG_CUDA(cudaMalloc(&E.tickets, MAX_TICKETS * sizeof(u32)));
     PG_CUDA(cudaMalloc(&E.err, 16));
     PG_CUDA(cudaMalloc(&E.plan_dev, sizeof(PlanOut)));

@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
             const u32 m = hi - lo;
             for (u32 e = tid; e < m; e += T) {
                 const u32 ent = q[e];
-                const u32 p = ent >> 16;
+                const u32 p = (ent >> 16) & (T - 1);  // in bounds even if a queue slot was left unwritten
                 Pos ch = sb[p];
                 make_move<S>(ch, (u16)(ent & 0xFFFFu));
                 ga.add(acc, sg[p], count_moves<1 - S, SL>(ch));
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32
             const u32 m = hi - lo;
             for (u32 e = tid; e < m; e += T) {
                 const u32 ent = q[e];
-                const u32 p = ent >> 16;
+                const u32 p = (ent >> 16) & (T - 1);  // in bounds even if a queue slot was left unwritten
                 Pos ch = sb[p];
                 make_move<S>(ch, (u16)(ent & 0xFFFFu));
                 const u64 o = chunk_out + lo + e;

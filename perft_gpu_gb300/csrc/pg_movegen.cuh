@@ -106,6 +106,16 @@ struct SlByteSmem {
     }
 };
 
+// hybrid: Kogge-Stone set-wise scans for the enemy's attacks, pins and checks
+// (ALU), fancy-magic lookups for the own sliders' moves (multiply on the FMA
+// pipe, table read on the load pipe), so the three pipes share the work
+struct SlHybrid {
+    static constexpr int kId = 3;
+    static constexpr bool kSetwise = true;
+    __device__ __forceinline__ static u64 bishop(int sq, u64 occ) { return SlFancy::bishop(sq, occ); }
+    __device__ __forceinline__ static u64 rook(int sq, u64 occ) { return SlFancy::rook(sq, occ); }
+};
+
 template <class SL> __device__ __forceinline__ void stage_tables()
 {
     if constexpr (SL::kId == 2) SlByteSmem::stage();
@@ -290,7 +300,7 @@ __device__ __noinline__ u32 count_ep_ks(const Pos& b, u64 pinned, u64 checkers)
 // line outside check and not at all in check.  The counts are the
 // reference's in every case (proved per term in the comments of the
 // reference-shaped paths above and checked bit-exact by the tests).
-template <int S>
+template <int S, bool OWN_BY_LOOKUP = false>
 __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
 {
     const u64 pawns = b.p & INNER;
@@ -339,28 +349,48 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
 
     u32 n = popc(king_set(king) & ~(threat | mine | xray));
 
-    // pass 2: own slider moves.  The propagator chains are rebuilt from an
-    // opaque copy of `empty` so the compiler does not keep pass 1's chains
-    // alive (a few more ALU operations for far fewer live registers).
-    u64 empty2 = empty;
-    asm volatile("" : "+l"(empty2));
     const u64 my_rq = b.rq & mine, my_bq = b.bq & mine;
     const u64 pin_chk = pinned & chk_all;
-    {
-        const u64 ns = my_rq & ~((pinned ^ lf.pinned) | pin_chk);
-        n += popc(Pro<8, true>(empty2).attacks(ns) & tgt) + popc(Pro<8, false>(empty2).attacks(ns) & tgt);
-    }
-    {
-        const u64 ew = my_rq & ~((pinned ^ lr.pinned) | pin_chk);
-        n += popc(Pro<1, true>(empty2).attacks(ew) & tgt) + popc(Pro<1, false>(empty2).attacks(ew) & tgt);
-    }
-    {
-        const u64 dg = my_bq & ~((pinned ^ ld.pinned) | pin_chk);
-        n += popc(Pro<9, true>(empty2).attacks(dg) & tgt) + popc(Pro<9, false>(empty2).attacks(dg) & tgt);
-    }
-    {
-        const u64 ad = my_bq & ~((pinned ^ la.pinned) | pin_chk);
-        n += popc(Pro<7, true>(empty2).attacks(ad) & tgt) + popc(Pro<7, false>(empty2).attacks(ad) & tgt);
+    if constexpr (OWN_BY_LOOKUP) {
+        // pass 2 by table lookup, one per own slider; a pinned piece keeps the
+        // moves along its pin line (none if the line is not its kind)
+        const int ksq = lsb(king) & 63;
+        for (u64 s = my_rq & ~pin_chk; s; s &= s - 1) {
+            const int sq = lsb(s);
+            const u64 bit = 1ull << sq;
+            u64 m = SlFancy::rook(sq, b.k | pawns | b.n | b.bq | b.rq) & tgt;
+            if (pinned & bit) m &= (lf.pinned & bit) ? file_of(ksq) : (lr.pinned & bit) ? rank_of(ksq) : 0ull;
+            n += popc(m);
+        }
+        for (u64 s = my_bq & ~pin_chk; s; s &= s - 1) {
+            const int sq = lsb(s);
+            const u64 bit = 1ull << sq;
+            u64 m = SlFancy::bishop(sq, b.k | pawns | b.n | b.bq | b.rq) & tgt;
+            if (pinned & bit) m &= (ld.pinned & bit) ? diag_of(ksq) : (la.pinned & bit) ? anti_of(ksq) : 0ull;
+            n += popc(m);
+        }
+    } else {
+        // pass 2: own slider moves.  The propagator chains are rebuilt from an
+        // opaque copy of `empty` so the compiler does not keep pass 1's chains
+        // alive (a few more ALU operations for far fewer live registers).
+        u64 empty2 = empty;
+        asm volatile("" : "+l"(empty2));
+        {
+            const u64 ns = my_rq & ~((pinned ^ lf.pinned) | pin_chk);
+            n += popc(Pro<8, true>(empty2).attacks(ns) & tgt) + popc(Pro<8, false>(empty2).attacks(ns) & tgt);
+        }
+        {
+            const u64 ew = my_rq & ~((pinned ^ lr.pinned) | pin_chk);
+            n += popc(Pro<1, true>(empty2).attacks(ew) & tgt) + popc(Pro<1, false>(empty2).attacks(ew) & tgt);
+        }
+        {
+            const u64 dg = my_bq & ~((pinned ^ ld.pinned) | pin_chk);
+            n += popc(Pro<9, true>(empty2).attacks(dg) & tgt) + popc(Pro<9, false>(empty2).attacks(dg) & tgt);
+        }
+        {
+            const u64 ad = my_bq & ~((pinned ^ la.pinned) | pin_chk);
+            n += popc(Pro<7, true>(empty2).attacks(ad) & tgt) + popc(Pro<7, false>(empty2).attacks(ad) & tgt);
+        }
     }
 
     for (u64 s = b.n & mine & ~pinned; s; s &= s - 1) n += popc(__ldg(&g_knight[lsb(s)]) & tgt);
@@ -473,7 +503,8 @@ __device__ __forceinline__ u32 count_moves_mg(const Pos& b)
 template <int S, class SL>
 __device__ __forceinline__ u32 count_moves(const Pos& b)
 {
-    if constexpr (SL::kId == 0) return count_moves_ks<S>(b);
+    if constexpr (SL::kId == 0) return count_moves_ks<S, false>(b);
+    else if constexpr (SL::kId == 3) return count_moves_ks<S, true>(b);
     else return count_moves_mg<S, SL>(b);
 }
 

@@ -30,10 +30,14 @@ struct SliderOps {
 extern const SliderOps g_ops_ks;
 extern const SliderOps g_ops_fancy;
 extern const SliderOps g_ops_byte;
+extern const SliderOps g_ops_hybrid;
 
 inline const SliderOps& ops_for(int slider)
 {
-    return slider == PG_SLIDER_FANCY ? g_ops_fancy : slider == PG_SLIDER_BYTE_SMEM ? g_ops_byte : g_ops_ks;
+    return slider == PG_SLIDER_FANCY       ? g_ops_fancy
+           : slider == PG_SLIDER_BYTE_SMEM ? g_ops_byte
+           : slider == PG_SLIDER_HYBRID    ? g_ops_hybrid
+                                           : g_ops_ks;
 }
 
 }  // namespace pg

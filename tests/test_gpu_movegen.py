@@ -15,7 +15,7 @@ def _walk():
     return g, boards
 
 
-@pytest.mark.parametrize("slider", ["ks", "fancy", "byte"])
+@pytest.mark.parametrize("slider", ["ks", "fancy", "byte", "hybrid"])
 def test_count_moves_batch_matches_reference(pg, slider):
     g, boards = _walk()
     pg.shutdown()

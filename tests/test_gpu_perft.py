@@ -8,7 +8,7 @@ from conftest import golden_json, golden_npz, words_of_hex
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("slider", ["ks", "fancy", "byte"])
+@pytest.mark.parametrize("slider", ["ks", "fancy", "byte", "hybrid"])
 def test_reference_fens_perft(pg, slider):
     for item in golden_json("fens.json"):
         b = pg.board_from_fen(item["fen"])
@@ -130,7 +130,7 @@ def test_autotuner_choices_and_auto_counts(pg):
     t = pg.autotune()
     assert t["leaf_plies"] in (1, 2) and t["seconds"] > 0
     for d, c in t["per_depth"].items():
-        assert c["slider"] in ("ks", "fancy", "byte") and c["block_size"] in (128, 256, 512)
+        assert c["slider"] in ("ks", "fancy", "byte", "hybrid") and c["block_size"] in (128, 256, 512)
         assert c["calibration_leaves_per_s"] > 0
     g = golden_npz("config3.npz")
     idx = np.arange(0, 4096, 29)
