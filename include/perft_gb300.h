@@ -142,7 +142,8 @@ int pg_perft_batch_device(const pg_board *d_pos, const uint8_t *d_depths, uint32
  * allocating call.  Limits: n <= 65536 positions, depths 0..3, and at most
  * 1,048,576 children of the depth-3 positions; larger requests return
  * PG_ERR_CAPACITY before any work.  The first call on a device looks up the
- * array's device address and uploads one small table; make that first call
+ * array's device address and uploads the move tables (about 0.9 MB, into
+ * file-scope device arrays of this library); make that first call
  * before any stream capture.  stream may be NULL (the default stream); the
  * call returns when d_out is written.  Every call reuses the same array, so
  * calls that overlap on the GPU (other threads, other streams) race.  Does

@@ -17,8 +17,8 @@
 // colour branches (S is a template parameter and frontier ranges are
 // side-uniform), own slider moves counted set-wise per direction with the
 // Kogge-Stone policy (rays of different sliders along one direction are
-// disjoint, so the popcounts add up exactly), and pins found from the king's
-// four lines without lookup tables.
+// disjoint, so the popcounts add up exactly), and pins and checks found
+// from the king's rays (two magic lookups) met by the enemy sliders' fills.
 #pragma once
 #include "pg_board.cuh"
 #include "pg_tables.h"
@@ -38,6 +38,18 @@ static __device__ u64 g_magic_attacks[MAGIC_TABLE_ENTRIES];
 static __device__ __align__(16) unsigned char g_magic_bytes[MAGIC_TABLE_ENTRIES];
 static __device__ u64 g_magic_unique[UNIQUE_TOTAL];
 static __device__ u64 g_knight[64];
+
+// uploads this translation unit's copy of the tables
+static inline cudaError_t upload_static_tables(const HostTables& t)
+{
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbol(g_magic_rook, t.rook, sizeof(t.rook)))) return e;
+    if ((e = cudaMemcpyToSymbol(g_magic_bishop, t.bishop, sizeof(t.bishop)))) return e;
+    if ((e = cudaMemcpyToSymbol(g_magic_attacks, t.attacks.data(), t.attacks.size() * sizeof(u64)))) return e;
+    if ((e = cudaMemcpyToSymbol(g_magic_bytes, t.bytes.data(), t.bytes.size()))) return e;
+    if ((e = cudaMemcpyToSymbol(g_magic_unique, t.unique.data(), t.unique.size() * sizeof(u64)))) return e;
+    return cudaMemcpyToSymbol(g_knight, t.knight, sizeof(t.knight));
+}
 
 // Kogge-Stone: pure shift/and/or, no memory traffic.
 struct SlKS {
@@ -243,33 +255,11 @@ template <int S, class SL> __device__ __forceinline__ u64 checkers(const Pos& b,
 // countMoves
 // ---------------------------------------------------------------------------
 
-// One line through the king (two opposite directions that share a step),
-// scanned with the propagator chains of those directions: the enemy sliders'
-// fills give the attacked squares, the king's own fills give its first
-// blockers, and their intersection gives pins and checks without a branch.
-struct LineScan {
-    u64 threat;    // enemy slider attacks along the line (king on the board)
-    u64 pinned;    // own pieces pinned along this line
-    u64 checkers;  // enemy sliders giving check along this line
-    u64 chk_ray;   // squares from the king to each such checker, checker included
-    u64 xray;      // the square beyond the king, away from a checker
-};
-
-template <int SH>
-__device__ __forceinline__ LineScan scan_line(const Pro<SH, true>& up_, const Pro<SH, false>& dn, u64 sliders,
-                                              u64 king, u64 mine)
+// Enemy slider attacks along one line kind (both directions of one step),
+// filled through `empty`.
+template <int SH> __device__ __forceinline__ u64 line_fill(u64 empty, u64 sliders)
 {
-    LineScan o;
-    const u64 a_up = up_.attacks(sliders), a_dn = dn.attacks(sliders);
-    const u64 k_up = up_.attacks(king), k_dn = dn.attacks(king);
-    o.threat = a_up | a_dn;
-    o.pinned = ((k_up & a_dn) | (k_dn & a_up)) & mine;
-    const u64 c_up = k_up & sliders, c_dn = k_dn & sliders;
-    o.checkers = c_up | c_dn;
-    o.chk_ray = (c_up ? k_up : 0ull) | (c_dn ? k_dn : 0ull);
-    o.xray = (c_up ? (shf<SH, false>(king) & DirMask<SH, false>::keep) : 0ull) |
-             (c_dn ? (shf<SH, true>(king) & DirMask<SH, true>::keep) : 0ull);
-    return o;
+    return Pro<SH, true>(empty).attacks(sliders) | Pro<SH, false>(empty).attacks(sliders);
 }
 
 // en passant for the branch-free count (rare: the file is set only when a
@@ -312,61 +302,65 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     const u64 trq = b.rq & theirs, tbq = b.bq & theirs;
     const u64 tp = pawns & theirs, tn = b.n & theirs;
 
-    // pass 1: enemy fills and king fills per line (pins, checks, x-rays)
-    LineScan lf, lr, ld, la;
-    {
-        const Pro<8, true> a(empty);
-        const Pro<8, false> c(empty);
-        lf = scan_line(a, c, trq, king, mine);
-    }
-    {
-        const Pro<1, true> a(empty);
-        const Pro<1, false> c(empty);
-        lr = scan_line(a, c, trq, king, mine);
-    }
-    {
-        const Pro<9, true> a(empty);
-        const Pro<9, false> c(empty);
-        ld = scan_line(a, c, tbq, king, mine);
-    }
-    {
-        const Pro<7, true> a(empty);
-        const Pro<7, false> c(empty);
-        la = scan_line(a, c, tbq, king, mine);
-    }
+    // pass 1: enemy slider fills per line kind, with the king taken off the
+    // board so that the squares behind it on a checking line are attacked
+    const u64 et = empty | king;
+    const u64 a_v = line_fill<8>(et, trq), a_h = line_fill<1>(et, trq);
+    const u64 a_d = line_fill<9>(et, tbq), a_a = line_fill<7>(et, tbq);
 
-    const u64 pinned = lf.pinned | lr.pinned | ld.pinned | la.pinned;
+    // the king's rays (first blockers included): one rook and one bishop
+    // lookup, split into the four lines
+    const int ksq = lsb(king) & 63;
+    const u64 kr = SlFancy::rook(ksq, occ), kb = SlFancy::bishop(ksq, occ);
+    const u64 kf = kr & file_of(ksq), kd = kb & diag_of(ksq);
+    const u64 kh = kr ^ kf, ka = kb ^ kd;
+
+    // A first blocker of the king on a line is pinned when an enemy slider
+    // attacks it along that line: nothing lies between the king and it, so
+    // the attack comes from beyond it.  With the king transparent, a slider
+    // checking along a line also reaches the king's first blocker on the far
+    // side; that piece can neither capture the checker nor block (every route
+    // onto the checking line crosses the king), and pinned pieces do not move
+    // in check, so the count is the same.
+    const u64 pf = kf & a_v & mine, pr = kh & a_h & mine, pd = kd & a_d & mine, pa = ka & a_a & mine;
+    const u64 pinned = pf | pr | pd | pa;
+    const u64 cr = kr & trq, cb = kb & tbq;
     const u64 nchk = knight_set(king) & tn;
     const u64 pchk = pawn_attackers_of<S>(king) & tp;
-    const u64 checkers = lf.checkers | lr.checkers | ld.checkers | la.checkers | nchk | pchk;
-    const u64 threat = lf.threat | lr.threat | ld.threat | la.threat | pawn_attacks<1 - S>(tp) | knight_set(tn) |
-                       king_set(b.k & theirs);
-    const u64 xray = lf.xray | lr.xray | ld.xray | la.xray;
-    const u64 safe = lf.chk_ray | lr.chk_ray | ld.chk_ray | la.chk_ray | nchk | pchk;
+    const u64 csl = cr | cb;
+    const u64 checkers = csl | nchk | pchk;
+    // single slider check: the squares between the king and the checker are
+    // where the king's rays meet the checker's rays of the same kind (the
+    // other lines of the two pieces are parallel); looked up unconditionally
+    // (a warp rarely agrees on being out of check) and dropped when no slider
+    // checks
+    const int csq = lsb(csl) & 63;
+    const u64 cray = SlFancy::look(cr ? g_magic_rook : g_magic_bishop, csq, occ) & (cr ? kr : kb);
+    const u64 safe = (csl ? cray : 0ull) | checkers;
+    const u64 threat = a_v | a_h | a_d | a_a | pawn_attacks<1 - S>(tp) | knight_set(tn) | king_set(b.k & theirs);
     const bool in_check = checkers != 0;
     const u64 chk_all = in_check ? ~0ull : 0ull;
     const u64 tgt = several(checkers) ? 0ull : (in_check ? safe : ~mine);
 
-    u32 n = popc(king_set(king) & ~(threat | mine | xray));
+    u32 n = popc(king_set(king) & ~(threat | mine));
 
     const u64 my_rq = b.rq & mine, my_bq = b.bq & mine;
     const u64 pin_chk = pinned & chk_all;
     if constexpr (OWN_BY_LOOKUP) {
         // pass 2 by table lookup, one per own slider; a pinned piece keeps the
         // moves along its pin line (none if the line is not its kind)
-        const int ksq = lsb(king) & 63;
         for (u64 s = my_rq & ~pin_chk; s; s &= s - 1) {
             const int sq = lsb(s);
             const u64 bit = 1ull << sq;
             u64 m = SlFancy::rook(sq, b.k | pawns | b.n | b.bq | b.rq) & tgt;
-            if (pinned & bit) m &= (lf.pinned & bit) ? file_of(ksq) : (lr.pinned & bit) ? rank_of(ksq) : 0ull;
+            if (pinned & bit) m &= (pf & bit) ? file_of(ksq) : (pr & bit) ? rank_of(ksq) : 0ull;
             n += popc(m);
         }
         for (u64 s = my_bq & ~pin_chk; s; s &= s - 1) {
             const int sq = lsb(s);
             const u64 bit = 1ull << sq;
             u64 m = SlFancy::bishop(sq, b.k | pawns | b.n | b.bq | b.rq) & tgt;
-            if (pinned & bit) m &= (ld.pinned & bit) ? diag_of(ksq) : (la.pinned & bit) ? anti_of(ksq) : 0ull;
+            if (pinned & bit) m &= (pd & bit) ? diag_of(ksq) : (pa & bit) ? anti_of(ksq) : 0ull;
             n += popc(m);
         }
     } else {
@@ -376,19 +370,19 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
         u64 empty2 = empty;
         asm volatile("" : "+l"(empty2));
         {
-            const u64 ns = my_rq & ~((pinned ^ lf.pinned) | pin_chk);
+            const u64 ns = my_rq & ~((pinned ^ pf) | pin_chk);
             n += popc(Pro<8, true>(empty2).attacks(ns) & tgt) + popc(Pro<8, false>(empty2).attacks(ns) & tgt);
         }
         {
-            const u64 ew = my_rq & ~((pinned ^ lr.pinned) | pin_chk);
+            const u64 ew = my_rq & ~((pinned ^ pr) | pin_chk);
             n += popc(Pro<1, true>(empty2).attacks(ew) & tgt) + popc(Pro<1, false>(empty2).attacks(ew) & tgt);
         }
         {
-            const u64 dg = my_bq & ~((pinned ^ ld.pinned) | pin_chk);
+            const u64 dg = my_bq & ~((pinned ^ pd) | pin_chk);
             n += popc(Pro<9, true>(empty2).attacks(dg) & tgt) + popc(Pro<9, false>(empty2).attacks(dg) & tgt);
         }
         {
-            const u64 ad = my_bq & ~((pinned ^ la.pinned) | pin_chk);
+            const u64 ad = my_bq & ~((pinned ^ pa) | pin_chk);
             n += popc(Pro<7, true>(empty2).attacks(ad) & tgt) + popc(Pro<7, false>(empty2).attacks(ad) & tgt);
         }
     }
@@ -402,12 +396,12 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     const u64 myp = pawns & mine;
     const u64 fp = myp & ~pinned;
     const u64 pin_ok = ~chk_all;
-    const u64 d1 = push1<S>(fp | (myp & lf.pinned & pin_ok)) & empty;
+    const u64 d1 = push1<S>(fp | (myp & pf & pin_ok)) & empty;
     const u64 s1 = d1 & tgt;
     n += popc(s1) + 3 * popc(s1 & BACK_RANKS);
     n += popc(push1<S>(d1 & double_rank<S>() & ~safe) & empty & tgt);
-    const u64 cw = cap_w<S>(fp | (myp & (S ? ld.pinned : la.pinned) & pin_ok)) & theirs & tgt;
-    const u64 ce = cap_e<S>(fp | (myp & (S ? la.pinned : ld.pinned) & pin_ok)) & theirs & tgt;
+    const u64 cw = cap_w<S>(fp | (myp & (S ? pd : pa) & pin_ok)) & theirs & tgt;
+    const u64 ce = cap_e<S>(fp | (myp & (S ? pa : pd) & pin_ok)) & theirs & tgt;
     n += popc(cw) + popc(ce) + 3 * (popc(cw & BACK_RANKS) + popc(ce & BACK_RANKS));
 
     if (!in_check) n += can_castle_k<S>(b, occ, threat) + can_castle_q<S>(b, occ, threat);

@@ -111,8 +111,9 @@ NaViews views(unsigned char* s)
     return v;
 }
 
-// per-device set-up: the scratch array's device address and the knight
-// table of this translation unit (the Kogge-Stone policy needs no other)
+// per-device set-up: the scratch array's device address and this
+// translation unit's copy of the move tables (knight moves, and the magic
+// tables the count reads the king's rays from)
 int na_setup(int dev, NaDevice*& out)
 {
     std::lock_guard<std::mutex> lk(g_na_mu);
@@ -125,16 +126,14 @@ int na_setup(int dev, NaDevice*& out)
             set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed: %s", cudaGetErrorString(e));
             return PG_ERR_CUDA;
         }
-        u64 knight[64];
-        for (int s = 0; s < 64; s++) {
-            const u64 b = 1ull << s;
-            const u64 a = ((b >> 1) & ~FILE_H) | ((b << 1) & ~FILE_A);
-            const u64 c = ((b >> 2) & 0x3F3F3F3F3F3F3F3Full) | ((b << 2) & 0xFCFCFCFCFCFCFCFCull);
-            knight[s] = (a << 16) | (a >> 16) | (c << 8) | (c >> 8);
+        const HostTables* t = host_tables();
+        if (!t) {
+            set_error("move table construction failed");
+            return PG_ERR_CUDA;
         }
-        e = cudaMemcpyToSymbol(g_knight, knight, sizeof(knight));
+        e = upload_static_tables(*t);
         if (e != cudaSuccess) {
-            set_error("knight table upload failed: %s", cudaGetErrorString(e));
+            set_error("move table upload failed: %s", cudaGetErrorString(e));
             return PG_ERR_CUDA;
         }
         e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);

@@ -30,13 +30,7 @@ inline int occupancy_grid(const void* fn, int T, int smem, u64 items, int num_sm
 template <class SL>
 cudaError_t upload_tables(const HostTables& t)
 {
-    cudaError_t e;
-    if ((e = cudaMemcpyToSymbol(g_magic_rook, t.rook, sizeof(t.rook)))) return e;
-    if ((e = cudaMemcpyToSymbol(g_magic_bishop, t.bishop, sizeof(t.bishop)))) return e;
-    if ((e = cudaMemcpyToSymbol(g_magic_attacks, t.attacks.data(), t.attacks.size() * sizeof(u64)))) return e;
-    if ((e = cudaMemcpyToSymbol(g_magic_bytes, t.bytes.data(), t.bytes.size()))) return e;
-    if ((e = cudaMemcpyToSymbol(g_magic_unique, t.unique.data(), t.unique.size() * sizeof(u64)))) return e;
-    return cudaMemcpyToSymbol(g_knight, t.knight, sizeof(t.knight));
+    return upload_static_tables(t);
 }
 
 template <class K> cudaError_t set_smem(K fn, int bytes)

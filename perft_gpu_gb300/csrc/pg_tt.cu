@@ -233,7 +233,7 @@ int tt_upload_keys()
         set_error("table construction failed");
         return PG_ERR_CUDA;
     }
-    TT_CUDA(cudaMemcpyToSymbol(g_knight, t->knight, sizeof(t->knight)));
+    TT_CUDA(upload_static_tables(*t));
     g_tt.keys_ready = true;
     return PG_OK;
 }
