@@ -280,6 +280,105 @@ def serve_leg(pg, rates, seconds, plain_rate):
     return out
 
 
+def _golden_json(name):
+    with open(os.path.join(ROOT, "tests", "golden", name)) as f:
+        return json.load(f)
+
+
+def _timed(fn):
+    t0 = time.perf_counter()
+    r = fn()
+    return r, time.perf_counter() - t0
+
+
+def workloads_leg(pg, threads):
+    """One timed pass of each of the other workloads, every count checked:
+    the 64-position depth-5 set (GPU batch, and the reference's CPU perft on
+    all host threads and on one), the single deep position at depth 7 under
+    every slider policy and with the TT, and the transposition-table workload
+    (that position at depth 8 and 256 playout positions at depth 7, TT against
+    no TT)."""
+    out = {}
+    # 64 positions at depth 5
+    c1 = _golden_json("config1.json")
+    b1 = pg.boards_array([pg.HexaBitBoardPosition(*(int(h, 16) for h in p["board"])) for p in c1["positions"]])
+    d1 = np.array([p["depth"] for p in c1["positions"]], dtype=np.uint8)
+    pg.perft_batch(b1, d1)
+    st = pg.PgStats()
+    r1, s1 = _timed(lambda: pg.perft_batch(b1, d1, stats=st))
+    assert int(r1.sum()) == c1["total"]
+    cpu_all = cpu_leaves_per_s(b1, d1, threads)
+    cpu_one = cpu_leaves_per_s(b1, d1, 1)
+    assert int(cpu_all[0].sum()) == c1["total"] and int(cpu_one[0].sum()) == c1["total"]
+    out["64_positions_depth5"] = {
+        "leaves": c1["total"], "gpu_leaves_per_s": c1["total"] / s1, "gpu_wall_s": s1,
+        "gpu_device_ms": st.device_ms,
+        "cpu": {"kind": cpu_all[2], "threads": threads, "leaves_per_s": c1["total"] / cpu_all[1],
+                "one_thread_leaves_per_s": c1["total"] / cpu_one[1]}}
+
+    # one deep position (seed 2, 30 plies, >= 35 moves) at depth 7
+    c2 = _golden_json("config2.json")
+    b2 = pg.HexaBitBoardPosition(*(int(h, 16) for h in c2["board"]))
+    rows = {}
+    for sl in ("ks", "fancy", "byte", "hybrid", "auto"):
+        pg.perft(b2, 6, slider=sl)
+        st = pg.PgStats()
+        r, s = _timed(lambda: pg.perft(b2, 7, slider=sl, stats=st))
+        assert r == c2["perft7"], (sl, r)
+        rows[sl] = {"leaves_per_s": r / s, "wall_s": s, "device_ms": st.device_ms,
+                    "leaf_kernel_ms": st.leaf_kernel_ms, "launches": st.launches}
+    pg.tt_clear()
+    st = pg.PgStats()
+    r, s = _timed(lambda: pg.perft(b2, 7, use_tt=True, stats=st))
+    assert r == c2["perft7"]
+    rows["tt"] = {"leaves_per_s": r / s, "wall_s": s, "device_ms": st.device_ms, "tt_probes": st.tt_probes,
+                  "tt_hits": st.tt_hits, "tt_stores": st.tt_stores}
+    out["single_position_depth7"] = {"leaves": c2["perft7"], "by_slider": rows}
+
+    # the README's own figure: "position 2" (perft.cu:64) without TT, 27 G
+    # leaf nodes/s on an overclocked GTX 780; depth 7 here, the count checked
+    # by agreement of the engine's slider policies (depth 5 is in the goldens)
+    fen2 = [f for f in _golden_json("fens.json") if f["name"] == "position2"][0]
+    p2 = pg.board_from_fen(fen2["fen"])
+    assert pg.perft(p2, 5) == fen2["perft"]["5"]
+    pg.perft(p2, 6)
+    st = pg.PgStats()
+    r7, s7 = _timed(lambda: pg.perft(p2, 7, stats=st))
+    assert r7 == pg.perft(p2, 7, slider="fancy")
+    out["position2_depth7"] = {"leaves": r7, "leaves_per_s": r7 / s7, "wall_s": s7, "device_ms": st.device_ms,
+                               "readme_gtx780_leaves_per_s": 27e9,
+                               "note": "README figure is one overclocked GTX 780 (Kepler); not the same hardware"}
+
+    # transposition-table workload: TT counts equal the no-TT counts
+    tt = {}
+    pg.tt_clear()
+    st = pg.PgStats()
+    r_tt, s_tt = _timed(lambda: pg.perft(b2, 8, use_tt=True, stats=st))
+    st0 = pg.PgStats()
+    r_no, s_no = _timed(lambda: pg.perft(b2, 8, stats=st0))
+    assert r_tt == r_no
+    tt["position_depth8"] = {"leaves": r_tt, "tt_s": s_tt, "no_tt_s": s_no, "speedup": s_no / s_tt,
+                             "tt_probes": st.tt_probes, "tt_hits": st.tt_hits, "tt_stores": st.tt_stores,
+                             "tt_entry_gb_per_s": (st.tt_probes + st.tt_stores) * 16 / (st.device_ms / 1e3) / 1e9
+                             if st.device_ms else None}
+    c4 = np.load(os.path.join(ROOT, "tests", "golden", "config4_d5.npz"))
+    b4 = c4["boards"].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    d4 = np.full(len(b4), 7, dtype=np.uint8)
+    pg.tt_clear()
+    st = pg.PgStats()
+    o_tt, s_tt = _timed(lambda: pg.perft_batch(b4, d4, use_tt=True, stats=st))
+    o_no, s_no = _timed(lambda: pg.perft_batch(b4, d4))
+    assert np.array_equal(o_tt, o_no)
+    tt["256_positions_depth7"] = {"leaves": int(o_tt.sum()), "tt_s": s_tt, "no_tt_s": s_no, "speedup": s_no / s_tt,
+                                  "tt_probes": st.tt_probes, "tt_hits": st.tt_hits, "tt_stores": st.tt_stores,
+                                  "tt_entry_gb_per_s": (st.tt_probes + st.tt_stores) * 16 / (st.device_ms / 1e3) / 1e9
+                                  if st.device_ms else None}
+    tt["note"] = ("TT: 781 seeded Zobrist keys, per-depth tables of 16-byte XOR-verified entries (32 GiB "
+                  "in total); every TT count equals the no-TT count")
+    out["transposition_table"] = tt
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local, dist = dist_setup()
@@ -426,6 +525,10 @@ def run_ours(args):
                    "peak_source": "2 ALU warp-instructions/clk/SM x 152 SMs x 2.07 GHz (nominal)",
                    "source": tj["source"]}
 
+        workloads = None
+        if not args.no_workloads:
+            workloads = workloads_leg(pg, os.cpu_count() or 1)
+
         served = None
         if not args.no_serve:
             rates = [float(x) for x in args.serve_rates.split(",")]
@@ -475,6 +578,7 @@ def run_ours(args):
                             "share_of_timed": leaf_ms / (elapsed * 1e3)},
             "cpu_baseline": cpu,
             "served": served,
+            "workloads": workloads,
             "clocks": clk,
         }
     barrier(dist)
@@ -492,12 +596,14 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--slider", default="auto", choices=["auto", "ks", "fancy", "byte"])
+    ap.add_argument("--slider", default="auto", choices=["auto", "ks", "fancy", "byte", "hybrid"])
     ap.add_argument("--cpu-stride", type=int, default=16,
                     help="CPU legs time every k-th position (bounded sample)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the other workloads (64 x depth 5, one position at depth 7, TT)")
     ap.add_argument("--serve-rates", default="25,50,100", help="Poisson request rates (req/s)")
     ap.add_argument("--serve-seconds", type=float, default=8.0)
     args = ap.parse_args()

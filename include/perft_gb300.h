@@ -57,7 +57,7 @@ typedef enum pg_slider {
     PG_SLIDER_KOGGE_STONE = 1,
     PG_SLIDER_FANCY = 2,     /* fancy magics, attack table in global memory (L2) */
     PG_SLIDER_BYTE_SMEM = 3, /* byte-lookup fancy magics staged in shared memory */
-    PG_SLIDER_HYBRID = 4     /* Kogge-Stone scans for attacks/pins/checks, magic lookups for own moves */
+    PG_SLIDER_HYBRID = 4     /* Kogge-Stone enemy fills, magic lookups for the king and own sliders */
 } pg_slider;
 
 typedef struct pg_config {

@@ -2,7 +2,7 @@
 binary (perft.cu:14-164):
 
     python -m perft_gpu_gb300 [<fen>] [<depth>] [<numGPUs>] [<launchDepth>]
-                              [--min-depth D] [--divide] [--slider ks|fancy|byte]
+                              [--min-depth D] [--divide] [--slider ks|fancy|byte|hybrid]
                               [--tt]
 
 Like perft.cu it runs perft for every depth from the minimum (3) to <depth>
@@ -31,7 +31,7 @@ def main(argv=None) -> int:
     ap.add_argument("launch_depth", nargs="?", type=int, default=0)
     ap.add_argument("--min-depth", type=int, default=3)
     ap.add_argument("--divide", action="store_true")
-    ap.add_argument("--slider", default="auto", choices=["auto", "ks", "fancy", "byte"])
+    ap.add_argument("--slider", default="auto", choices=["auto", "ks", "fancy", "byte", "hybrid"])
     ap.add_argument("--tt", action="store_true", help="use the transposition tables")
     a = ap.parse_args(argv)
     if a.num_gpus != 1:
