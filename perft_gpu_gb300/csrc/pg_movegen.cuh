@@ -38,6 +38,7 @@ static __device__ u64 g_magic_attacks[MAGIC_TABLE_ENTRIES];
 static __device__ __align__(16) unsigned char g_magic_bytes[MAGIC_TABLE_ENTRIES];
 static __device__ u64 g_magic_unique[UNIQUE_TOTAL];
 static __device__ u64 g_knight[64];
+static __device__ u64 g_king[64];
 
 // uploads this translation unit's copy of the tables
 static inline cudaError_t upload_static_tables(const HostTables& t)
@@ -48,6 +49,7 @@ static inline cudaError_t upload_static_tables(const HostTables& t)
     if ((e = cudaMemcpyToSymbol(g_magic_attacks, t.attacks.data(), t.attacks.size() * sizeof(u64)))) return e;
     if ((e = cudaMemcpyToSymbol(g_magic_bytes, t.bytes.data(), t.bytes.size()))) return e;
     if ((e = cudaMemcpyToSymbol(g_magic_unique, t.unique.data(), t.unique.size() * sizeof(u64)))) return e;
+    if ((e = cudaMemcpyToSymbol(g_king, t.king, sizeof(t.king)))) return e;
     return cudaMemcpyToSymbol(g_knight, t.knight, sizeof(t.knight));
 }
 
@@ -325,7 +327,7 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     const u64 pf = kf & a_v & mine, pr = kh & a_h & mine, pd = kd & a_d & mine, pa = ka & a_a & mine;
     const u64 pinned = pf | pr | pd | pa;
     const u64 cr = kr & trq, cb = kb & tbq;
-    const u64 nchk = knight_set(king) & tn;
+    const u64 nchk = __ldg(&g_knight[ksq]) & tn;
     const u64 pchk = pawn_attackers_of<S>(king) & tp;
     const u64 csl = cr | cb;
     const u64 checkers = csl | nchk | pchk;
@@ -337,12 +339,13 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     const int csq = lsb(csl) & 63;
     const u64 cray = SlFancy::look(cr ? g_magic_rook : g_magic_bishop, csq, occ) & (cr ? kr : kb);
     const u64 safe = (csl ? cray : 0ull) | checkers;
-    const u64 threat = a_v | a_h | a_d | a_a | pawn_attacks<1 - S>(tp) | knight_set(tn) | king_set(b.k & theirs);
+    const u64 threat = a_v | a_h | a_d | a_a | pawn_attacks<1 - S>(tp) | knight_set(tn) |
+                       __ldg(&g_king[lsb(b.k & theirs) & 63]);
     const bool in_check = checkers != 0;
     const u64 chk_all = in_check ? ~0ull : 0ull;
     const u64 tgt = several(checkers) ? 0ull : (in_check ? safe : ~mine);
 
-    u32 n = popc(king_set(king) & ~(threat | mine));
+    u32 n = popc(__ldg(&g_king[ksq]) & ~(threat | mine));
 
     const u64 my_rq = b.rq & mine, my_bq = b.bq & mine;
     const u64 pin_chk = pinned & chk_all;
@@ -431,12 +434,12 @@ __device__ __forceinline__ u32 count_moves_mg(const Pos& b)
     const u64 trq = b.rq & theirs, tbq = b.bq & theirs;
     const u64 tp = pawns & theirs, tn = b.n & theirs;
 
-    u64 threat = pawn_attacks<1 - S>(tp) | knight_set(tn) | king_set(b.k & theirs);
+    u64 threat = pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[lsb(b.k & theirs) & 63]);
     for (u64 s = trq; s; s &= s - 1) threat |= SL::rook(lsb(s), occ);
     for (u64 s = tbq; s; s &= s - 1) threat |= SL::bishop(lsb(s), occ);
 
     const u64 ra = SL::rook(ksq, occ), ba = SL::bishop(ksq, occ);
-    const u64 nchk = knight_set(king) & tn;
+    const u64 nchk = __ldg(&g_knight[ksq]) & tn;
     const u64 pchk = pawn_attackers_of<S>(king) & tp;
     const u64 schk = (ra & trq) | (ba & tbq);
     const u64 checkers = schk | nchk | pchk;
@@ -459,7 +462,7 @@ __device__ __forceinline__ u32 count_moves_mg(const Pos& b)
     const bool in_check = checkers != 0;
     const u64 chk_all = in_check ? ~0ull : 0ull;
     const u64 tgt = several(checkers) ? 0ull : (in_check ? safe : ~mine);
-    u32 n = popc(king_set(king) & ~(threat | behind | mine));
+    u32 n = popc(__ldg(&g_king[ksq]) & ~(threat | behind | mine));
 
     const u64 lf = file_of(ksq), lr = rank_of(ksq), ld = diag_of(ksq), la = anti_of(ksq);
     const u64 stay = pinned & chk_all;  // in check a pinned piece never moves

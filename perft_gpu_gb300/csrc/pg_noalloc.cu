@@ -112,7 +112,7 @@ NaViews views(unsigned char* s)
 }
 
 // per-device set-up: the scratch array's device address and this
-// translation unit's copy of the move tables (knight moves, and the magic
+// translation unit's copy of the move tables (knight and king moves, and the magic
 // tables the count reads the king's rays from)
 int na_setup(int dev, NaDevice*& out)
 {

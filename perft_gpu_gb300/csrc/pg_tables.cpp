@@ -123,6 +123,9 @@ int build_tables(HostTables& t)
         const u64 a = ((b >> 1) & ~(0x0101010101010101ull << 7)) | ((b << 1) & ~0x0101010101010101ull);
         const u64 c = ((b >> 2) & 0x3F3F3F3F3F3F3F3Full) | ((b << 2) & 0xFCFCFCFCFCFCFCFCull);
         t.knight[s] = (a << 16) | (a >> 16) | (c << 8) | (c >> 8);
+        const u64 row = b | a;
+        t.king[s] = ((b >> 1) & ~(0x0101010101010101ull << 7)) | ((b << 1) & ~0x0101010101010101ull) | (row << 8) |
+                    (row >> 8);
     }
     return 0;
 }

@@ -25,6 +25,7 @@ struct HostTables {
     std::vector<unsigned char> bytes;
     std::vector<u64> unique;
     u64 knight[64];
+    u64 king[64];
 };
 
 // built once per process; nullptr if the search failed
