@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
             const u32 hi = min(lo + (u32)QCAP, total);
             if (c && off < hi && off + c > lo) {
                 QEmit e{q, off, lo, hi, (u32)tid << 16};
-                gen_moves<S, SL>(b, e);
+                gen_leaf<S>(b, e);
             }
             __syncthreads();
             const u32 m = hi - lo;
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32
             const u32 hi = min(lo + (u32)QCAP, total);
             if (c && off < hi && off + c > lo) {
                 QEmit e{q, off, lo, hi, (u32)tid << 16};
-                gen_moves<S, SL>(bd, e);
+                gen_leaf<S>(bd, e);
             }
             __syncthreads();
             const u32 m = hi - lo;

@@ -285,16 +285,25 @@ __device__ __noinline__ u32 count_ep_ks(const Pos& b, u64 pinned, u64 checkers)
     return n;
 }
 
-// countMoves / countMovesOutOfCheck (MGB.h:3008-3295, 2825-3002) as one
-// instruction stream for the Kogge-Stone policy.  Check handling is a target
-// mask: ~own outside check, the check ray (between squares + checker) in
-// single check, nothing in double check; pinned pieces move along their pin
-// line outside check and not at all in check.  The counts are the
-// reference's in every case (proved per term in the comments of the
-// reference-shaped paths above and checked bit-exact by the tests).
-template <int S, bool OWN_BY_LOOKUP = false>
-__device__ __forceinline__ u32 count_moves_ks(const Pos& b)
+// What the count and the in-kernel generator need to know about a position,
+// computed without a branch: pins per line, checkers, the target mask and
+// the squares the enemy attacks with the side to move's king taken off the
+// board (findPinnedPieces / findAttackedSquares, MGB.h:1213-1298, in mask
+// form).
+template <int S> struct KsFacts {
+    u64 pawns, occ, mine, theirs, empty;
+    int ksq;
+    u64 pf, pr, pd, pa;  // own pieces pinned along the king's file / rank / diagonal / anti-diagonal
+    u64 pinned, checkers;
+    u64 safe;     // the check ray and the checkers (nothing out of check)
+    u64 threat;   // enemy attacks with the king transparent
+    u64 chk_all;  // all ones in check
+    u64 tgt;      // where non-king pieces may move: ~own, the check ray, or nothing
+};
+
+template <int S> __device__ __forceinline__ KsFacts<S> ks_facts(const Pos& b)
 {
+    KsFacts<S> f;
     const u64 pawns = b.p & INNER;
     const u64 occ = b.k | pawns | b.n | b.bq | b.rq;
     const u64 black = occ & ~b.w;
@@ -304,8 +313,8 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     const u64 trq = b.rq & theirs, tbq = b.bq & theirs;
     const u64 tp = pawns & theirs, tn = b.n & theirs;
 
-    // pass 1: enemy slider fills per line kind, with the king taken off the
-    // board so that the squares behind it on a checking line are attacked
+    // enemy slider fills per line kind, with the king taken off the board so
+    // that the squares behind it on a checking line are attacked
     const u64 et = empty | king;
     const u64 a_v = line_fill<8>(et, trq), a_h = line_fill<1>(et, trq);
     const u64 a_d = line_fill<9>(et, tbq), a_a = line_fill<7>(et, tbq);
@@ -323,14 +332,17 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     // checking along a line also reaches the king's first blocker on the far
     // side; that piece can neither capture the checker nor block (every route
     // onto the checking line crosses the king), and pinned pieces do not move
-    // in check, so the count is the same.
-    const u64 pf = kf & a_v & mine, pr = kh & a_h & mine, pd = kd & a_d & mine, pa = ka & a_a & mine;
-    const u64 pinned = pf | pr | pd | pa;
+    // in check, so the moves are the same.
+    f.pf = kf & a_v & mine;
+    f.pr = kh & a_h & mine;
+    f.pd = kd & a_d & mine;
+    f.pa = ka & a_a & mine;
+    f.pinned = f.pf | f.pr | f.pd | f.pa;
     const u64 cr = kr & trq, cb = kb & tbq;
     const u64 nchk = __ldg(&g_knight[ksq]) & tn;
     const u64 pchk = pawn_attackers_of<S>(king) & tp;
     const u64 csl = cr | cb;
-    const u64 checkers = csl | nchk | pchk;
+    f.checkers = csl | nchk | pchk;
     // single slider check: the squares between the king and the checker are
     // where the king's rays meet the checker's rays of the same kind (the
     // other lines of the two pieces are parallel); looked up unconditionally
@@ -338,12 +350,36 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     // checks
     const int csq = lsb(csl) & 63;
     const u64 cray = SlFancy::look(cr ? g_magic_rook : g_magic_bishop, csq, occ) & (cr ? kr : kb);
-    const u64 safe = (csl ? cray : 0ull) | checkers;
-    const u64 threat = a_v | a_h | a_d | a_a | pawn_attacks<1 - S>(tp) | knight_set(tn) |
-                       __ldg(&g_king[lsb(b.k & theirs) & 63]);
+    f.safe = (csl ? cray : 0ull) | f.checkers;
+    f.threat = a_v | a_h | a_d | a_a | pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[lsb(b.k & theirs) & 63]);
+    const bool in_check = f.checkers != 0;
+    f.chk_all = in_check ? ~0ull : 0ull;
+    f.tgt = several(f.checkers) ? 0ull : (in_check ? f.safe : ~mine);
+    f.pawns = pawns;
+    f.occ = occ;
+    f.mine = mine;
+    f.theirs = theirs;
+    f.empty = empty;
+    f.ksq = ksq;
+    return f;
+}
+
+// countMoves / countMovesOutOfCheck (MGB.h:3008-3295, 2825-3002) as one
+// instruction stream for the Kogge-Stone policy.  Check handling is a target
+// mask: ~own outside check, the check ray (between squares + checker) in
+// single check, nothing in double check; pinned pieces move along their pin
+// line outside check and not at all in check.  The counts are the
+// reference's in every case (proved per term in the comments of the
+// reference-shaped paths above and checked bit-exact by the tests).
+template <int S, bool OWN_BY_LOOKUP = false>
+__device__ __forceinline__ u32 count_moves_ks(const Pos& b)
+{
+    const KsFacts<S> f = ks_facts<S>(b);
+    const u64 pawns = f.pawns, occ = f.occ, mine = f.mine, theirs = f.theirs, empty = f.empty;
+    const u64 pf = f.pf, pr = f.pr, pd = f.pd, pa = f.pa, pinned = f.pinned, checkers = f.checkers;
+    const u64 safe = f.safe, threat = f.threat, chk_all = f.chk_all, tgt = f.tgt;
+    const int ksq = f.ksq;
     const bool in_check = checkers != 0;
-    const u64 chk_all = in_check ? ~0ull : 0ull;
-    const u64 tgt = several(checkers) ? 0ull : (in_check ? safe : ~mine);
 
     u32 n = popc(__ldg(&g_king[ksq]) & ~(threat | mine));
 
@@ -520,6 +556,75 @@ template <class E> __device__ __forceinline__ void emit_pawn(E& emit, int from, 
         emit(cmove(from, to, fl | MF_PROMO_R));
     } else {
         emit(cmove(from, to, fl));
+    }
+}
+
+// The legal moves counted by count_moves_ks, emitted in an order of our own
+// for the kernels that only need the set of children (the leaf and the level
+// expansion): king, knights, bishop/queen, rook/queen, pawn pushes, double
+// pushes, captures, castles, en passant.  Same analysis as the count, so the
+// number emitted equals the count for every position; the flags are the
+// reference's (double push, castles, en passant, promotions, captures).
+template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b, E& emit)
+{
+    const KsFacts<S> f = ks_facts<S>(b);
+    const u64 tgt = f.tgt;
+    const int ksq = f.ksq;
+    for (u64 m = __ldg(&g_king[ksq]) & ~(f.threat | f.mine); m; m &= m - 1)
+        emit(cmove(ksq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0));
+    const u64 pin_chk = f.pinned & f.chk_all;
+    for (u64 s = b.n & f.mine & ~f.pinned; s; s &= s - 1) {
+        const int sq = lsb(s);
+        for (u64 m = __ldg(&g_knight[sq]) & tgt; m; m &= m - 1)
+            emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0));
+    }
+    // a pinned slider keeps the moves along its pin line (none if the line is
+    // not its kind); in check pinned pieces do not move
+    for (u64 s = b.bq & f.mine & ~pin_chk; s; s &= s - 1) {
+        const int sq = lsb(s);
+        const u64 bit = lowbit(s);
+        u64 m = SlFancy::bishop(sq, f.occ) & tgt;
+        if (f.pinned & bit) m &= (f.pd & bit) ? diag_of(ksq) : (f.pa & bit) ? anti_of(ksq) : 0ull;
+        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0));
+    }
+    for (u64 s = b.rq & f.mine & ~pin_chk; s; s &= s - 1) {
+        const int sq = lsb(s);
+        const u64 bit = lowbit(s);
+        u64 m = SlFancy::rook(sq, f.occ) & tgt;
+        if (f.pinned & bit) m &= (f.pf & bit) ? file_of(ksq) : (f.pr & bit) ? rank_of(ksq) : 0ull;
+        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0));
+    }
+    // pawns, set-wise as in the count; from = to - step
+    constexpr int PUSH = S ? -8 : 8, CW = S ? -9 : 7, CE = S ? -7 : 9;
+    const u64 myp = f.pawns & f.mine;
+    const u64 fp = myp & ~f.pinned;
+    const u64 pin_ok = ~f.chk_all;
+    const u64 d1 = push1<S>(fp | (myp & f.pf & pin_ok)) & f.empty;
+    for (u64 m = d1 & tgt; m; m &= m - 1) emit_pawn(emit, lsb(m) - PUSH, lowbit(m), 0);
+    for (u64 m = push1<S>(d1 & double_rank<S>() & ~f.safe) & f.empty & tgt; m; m &= m - 1)
+        emit(cmove(lsb(m) - 2 * PUSH, lsb(m), MF_DOUBLE));
+    for (u64 m = cap_w<S>(fp | (myp & (S ? f.pd : f.pa) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
+        emit_pawn(emit, lsb(m) - CW, lowbit(m), MF_CAPTURE);
+    for (u64 m = cap_e<S>(fp | (myp & (S ? f.pa : f.pd) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
+        emit_pawn(emit, lsb(m) - CE, lowbit(m), MF_CAPTURE);
+    if (!f.checkers) {
+        if (can_castle_k<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 62 : 6, MF_KCASTLE));
+        if (can_castle_q<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 58 : 2, MF_QCASTLE));
+    }
+    // en passant: the rules of count_ep_ks
+    if (b.p & 0xF0ull) {
+        const u64 et = ep_target<S>(b);
+        const u64 victim = S ? up(et) : down(et);
+        const int to = lsb(et) & 63;
+        u64 cand = (east1(victim) | west1(victim)) & myp;
+        if (f.checkers) {
+            cand = (victim == f.checkers) ? (cand & ~f.pinned) : 0ull;
+            for (; cand; cand &= cand - 1) emit(cmove(lsb(cand), to, MF_EP));
+        } else {
+            const Sides<S> c(b);
+            for (; cand; cand &= cand - 1)
+                if (ep_legal<S>(c, f.pinned, lowbit(cand), et, victim)) emit(cmove(lsb(cand), to, MF_EP));
+        }
     }
 }
 
