@@ -565,18 +565,20 @@ template <class E> __device__ __forceinline__ void emit_pawn(E& emit, int from, 
 // pushes, captures, castles, en passant.  Same analysis as the count, so the
 // number emitted equals the count for every position; the flags are the
 // reference's (double push, castles, en passant, promotions, captures).
+// Non-pawn moves also pass the moving piece (PC_*) to the emitter.
+enum : u32 { PC_PAWN = 0, PC_KNIGHT = 1, PC_BISHOP = 2, PC_ROOK = 3, PC_QUEEN = 4, PC_KING = 5 };
 template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b, E& emit)
 {
     const KsFacts<S> f = ks_facts<S>(b);
     const u64 tgt = f.tgt;
     const int ksq = f.ksq;
     for (u64 m = __ldg(&g_king[ksq]) & ~(f.threat | f.mine); m; m &= m - 1)
-        emit(cmove(ksq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0));
+        emit(cmove(ksq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0), PC_KING);
     const u64 pin_chk = f.pinned & f.chk_all;
     for (u64 s = b.n & f.mine & ~f.pinned; s; s &= s - 1) {
         const int sq = lsb(s);
         for (u64 m = __ldg(&g_knight[sq]) & tgt; m; m &= m - 1)
-            emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0));
+            emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0), PC_KNIGHT);
     }
     // a pinned slider keeps the moves along its pin line (none if the line is
     // not its kind); in check pinned pieces do not move
@@ -585,14 +587,16 @@ template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b,
         const u64 bit = lowbit(s);
         u64 m = SlFancy::bishop(sq, f.occ) & tgt;
         if (f.pinned & bit) m &= (f.pd & bit) ? diag_of(ksq) : (f.pa & bit) ? anti_of(ksq) : 0ull;
-        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0));
+        const u32 pc = (b.rq & bit) ? PC_QUEEN : PC_BISHOP;
+        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0), pc);
     }
     for (u64 s = b.rq & f.mine & ~pin_chk; s; s &= s - 1) {
         const int sq = lsb(s);
         const u64 bit = lowbit(s);
         u64 m = SlFancy::rook(sq, f.occ) & tgt;
         if (f.pinned & bit) m &= (f.pf & bit) ? file_of(ksq) : (f.pr & bit) ? rank_of(ksq) : 0ull;
-        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0));
+        const u32 pc = (b.bq & bit) ? PC_QUEEN : PC_ROOK;
+        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0), pc);
     }
     // pawns, set-wise as in the count; from = to - step
     constexpr int PUSH = S ? -8 : 8, CW = S ? -9 : 7, CE = S ? -7 : 9;
@@ -608,8 +612,8 @@ template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b,
     for (u64 m = cap_e<S>(fp | (myp & (S ? f.pa : f.pd) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
         emit_pawn(emit, lsb(m) - CE, lowbit(m), MF_CAPTURE);
     if (!f.checkers) {
-        if (can_castle_k<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 62 : 6, MF_KCASTLE));
-        if (can_castle_q<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 58 : 2, MF_QCASTLE));
+        if (can_castle_k<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 62 : 6, MF_KCASTLE), PC_KING);
+        if (can_castle_q<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 58 : 2, MF_QCASTLE), PC_KING);
     }
     // en passant: the rules of count_ep_ks
     if (b.p & 0xF0ull) {
@@ -804,6 +808,51 @@ __device__ __forceinline__ void make_move(Pos& b, u16 mv)
     set_ep(b, 0);
     castle_update(b, dst, S);
     if (pieceIsRook) castle_update(b, src, 1 - S);
+    if (fl == MF_DOUBLE) {
+        const u64 pawns = b.p & INNER;
+        const u64 occ = b.k | pawns | b.n | b.bq | b.rq;
+        const u64 enemy = S ? b.w : (occ & ~b.w);
+        if ((east1(dst) | west1(dst)) & pawns & enemy) set_ep(b, (from & 7) + 1);
+    }
+}
+
+// makeMove for a child whose moves are only counted: it writes what the count
+// for the side to move next reads (the pieces, that side's castling rights
+// and the exact en-passant file, as make_move) and leaves the mover's own
+// castling rights and the side bit as they were.  `piece` is the moving piece
+// (PC_*), so nothing is looked up on the board to find it.
+template <int S>
+__device__ __forceinline__ void make_child(Pos& b, u16 mv, u32 piece)
+{
+    const int from = mv & 63, to = (mv >> 6) & 63, fl = (mv >> 12) & 15;
+    const u64 src = 1ull << from, dst = 1ull << to;
+    const bool promo = fl & 8;
+    const int pr = fl & 3;  // promotion piece: 0 N, 1 B, 2 R, 3 Q
+    const bool toN = promo ? pr == 0 : piece == PC_KNIGHT;
+    const bool toB = promo ? (pr & 1) != 0 : (piece == PC_BISHOP || piece == PC_QUEEN);
+    const bool toR = promo ? pr >= 2 : (piece == PC_ROOK || piece == PC_QUEEN);
+    const bool toP = !promo && piece == PC_PAWN;
+    const u64 clr = ~(src | dst);
+    b.bq = (b.bq & clr) | (toB ? dst : 0ull);
+    b.rq = (b.rq & clr) | (toR ? dst : 0ull);
+    b.n = (b.n & clr) | (toN ? dst : 0ull);
+    b.p = (b.p & ~((src | dst) & INNER)) | (toP ? dst : 0ull);
+    if (piece == PC_KING) b.k = (b.k ^ src) | dst;
+    b.w = S ? (b.w & ~dst) : ((b.w ^ src) | dst);
+    if (fl == MF_EP) {
+        const u64 victim = S ? up(dst) : down(dst);
+        b.p &= ~(victim & INNER);
+        if (S) b.w &= ~victim;
+    }
+    if (fl == MF_KCASTLE || fl == MF_QCASTLE) {
+        const int base = S ? 56 : 0;
+        const u64 rf = 1ull << (base + (fl == MF_KCASTLE ? 7 : 0));
+        const u64 rt = 1ull << (base + (fl == MF_KCASTLE ? 5 : 3));
+        b.rq = (b.rq ^ rf) | rt;
+        if (!S) b.w = (b.w ^ rf) | rt;
+    }
+    set_ep(b, 0);
+    castle_update(b, dst, S);  // a capture on the other side's rook corner
     if (fl == MF_DOUBLE) {
         const u64 pawns = b.p & INNER;
         const u64 occ = b.k | pawns | b.n | b.bq | b.rq;
