@@ -66,23 +66,24 @@ static TTState g_tt;
 // kernels
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ u64 zobrist_hash(const Pos& b)
+// z: the 781 keys (staged in shared memory by the caller)
+__device__ __forceinline__ u64 zobrist_hash(const Pos& b, const u64* z)
 {
     const u64 pawns = b.p & INNER;
     const u64 sets[6] = {pawns, b.n, b.bq & ~b.rq, b.rq & ~b.bq, b.bq & b.rq, b.k};
     u64 h = 0;
 #pragma unroll
     for (int t = 0; t < 6; t++) {
-        for (u64 s = sets[t] & b.w; s; s &= s - 1) h ^= __ldg(&g_zobrist[t * 64 + lsb(s)]);
-        for (u64 s = sets[t] & ~b.w; s; s &= s - 1) h ^= __ldg(&g_zobrist[(6 + t) * 64 + lsb(s)]);
+        for (u64 s = sets[t] & b.w; s; s &= s - 1) h ^= z[t * 64 + lsb(s)];
+        for (u64 s = sets[t] & ~b.w; s; s &= s - 1) h ^= z[(6 + t) * 64 + lsb(s)];
     }
     const int wc = st_wc(b), bc = st_bc(b), ep = st_ep(b);
-    if (wc & 1) h ^= __ldg(&g_zobrist[Z_CASTLE + 0]);
-    if (wc & 2) h ^= __ldg(&g_zobrist[Z_CASTLE + 1]);
-    if (bc & 1) h ^= __ldg(&g_zobrist[Z_CASTLE + 2]);
-    if (bc & 2) h ^= __ldg(&g_zobrist[Z_CASTLE + 3]);
-    if (ep) h ^= __ldg(&g_zobrist[Z_EP + ((ep - 1) & 7)]);
-    if (st_side(b)) h ^= __ldg(&g_zobrist[Z_SIDE]);
+    if (wc & 1) h ^= z[Z_CASTLE + 0];
+    if (wc & 2) h ^= z[Z_CASTLE + 1];
+    if (bc & 1) h ^= z[Z_CASTLE + 2];
+    if (bc & 2) h ^= z[Z_CASTLE + 3];
+    if (ep) h ^= z[Z_EP + ((ep - 1) & 7)];
+    if (st_side(b)) h ^= z[Z_SIDE];
     return h ? h : 1;  // 0 marks an empty slot of the duplicate table
 }
 
@@ -95,17 +96,34 @@ __device__ __forceinline__ u64 dd_key(u64 h, u32 rem)
 }
 __device__ __forceinline__ u32 dd_slot(u64 k, u64 mask) { return (u32)(((k >> 23) ^ (k >> 41) ^ k) & mask); }
 
+// Adds a per-thread count into *dst with one global atomic per CTA (the
+// threads of a warp are summed by a warp reduction, the warps in shared
+// memory); every thread of the CTA calls it.
+__device__ __forceinline__ void block_count_add(u64* dst, u32 v)
+{
+    __shared__ u32 s_sum;
+    if (threadIdx.x == 0) s_sum = 0;
+    __syncthreads();
+    const u32 w = __reduce_add_sync(0xFFFFFFFFu, v);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&s_sum, w);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_sum) atomicAdd(dst, (u64)s_sum);
+}
+
 // hash, TT probe, and first claim of the level's duplicate table
 static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TTSet tt, u64 dd_mask, u64* counters)
 {
-    u64 probes = 0, hits = 0;
+    __shared__ u64 z[ZOBRIST_KEYS];
+    for (int i = threadIdx.x; i < ZOBRIST_KEYS; i += blockDim.x) z[i] = g_zobrist[i];
+    __syncthreads();
+    u32 probes = 0, hits = 0;
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const u32 idx = start + i;
         const u32 rem = lv.rem[idx];
         lt.acc[idx] = 0;
         lt.dup[idx] = NO_DUP;
         if (rem < TT_MIN_DEPTH || rem >= REM_DEAD) continue;
-        const u64 h = zobrist_hash(load_board(lv, idx));
+        const u64 h = zobrist_hash(load_board(lv, idx), z);
         lt.hash[idx] = h;
         if (rem <= TT_MAX_DEPTH && tt.tab[rem]) {
             probes++;
@@ -122,8 +140,8 @@ static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TT
         const u64 prev = atomicCAS(&lt.dd_hash[s], 0ull, k);
         if (prev == 0 || prev == k) atomicMin(&lt.dd_idx[s], idx);
     }
-    if (probes) atomicAdd(&counters[0], probes);
-    if (hits) atomicAdd(&counters[1], hits);
+    block_count_add(&counters[0], probes);
+    block_count_add(&counters[1], hits);
 }
 
 // a node whose key was claimed first by another node of its level takes that
@@ -152,22 +170,47 @@ __device__ __forceinline__ void tt_store(const TTSet& tt, u32 rem, u64 h, u64 v)
     tt.tab[rem][h & tt.mask[rem]] = make_ulonglong2(h ^ v, v);
 }
 
-// children [0, m) of one chunk are final: store them and add them to parents
+// children [0, m) of one chunk are final: store them and add them to parents.
+// The expansion writes the children of a parent next to each other in parent
+// order, so a warp sums each run of equal parents (segmented shuffle
+// reduction) and adds it with one atomic; a warp whose parents are not in
+// order adds lane by lane.
 static __global__ void k_tt_upsweep(LevelView ch, u32 m, LevelTT ct, TTSet tt, u64* __restrict__ parent_acc,
                                     u64* counters)
 {
-    u64 stores = 0;
-    for (u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
-        const u32 d = ct.dup[j];
-        const u64 v = d != NO_DUP ? ct.acc[d] : ct.acc[j];
-        const u32 rem = ch.rem[j];
-        if (rem >= TT_MIN_DEPTH && rem <= TT_MAX_DEPTH && tt.tab[rem]) {
-            tt_store(tt, rem, ct.hash[j], v);
-            stores++;
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    const u32 lane = threadIdx.x & 31;
+    const u32 stride = gridDim.x * blockDim.x;  // a multiple of 32: every lane of a warp runs the same iterations
+    u32 stores = 0;
+    for (u32 base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < m; base += stride) {
+        const u32 j = base + lane;
+        const bool valid = j < m;
+        u64 v = 0;
+        u32 par = 0xFFFFFFFFu;
+        if (valid) {
+            const u32 d = ct.dup[j];
+            v = d != NO_DUP ? ct.acc[d] : ct.acc[j];
+            const u32 rem = ch.rem[j];
+            if (rem >= TT_MIN_DEPTH && rem <= TT_MAX_DEPTH && tt.tab[rem]) {
+                tt_store(tt, rem, ct.hash[j], v);
+                stores++;
+            }
+            par = ct.parent[j];
         }
-        atomicAdd(&parent_acc[ct.parent[j]], v);
+        const u32 prev = __shfl_up_sync(FULL, par, 1);
+        const u32 next = __shfl_down_sync(FULL, par, 1);
+        if (!__all_sync(FULL, lane == 31 || next >= par)) {
+            if (valid) atomicAdd(&parent_acc[par], v);
+            continue;
+        }
+        for (u32 o = 1; o < 32; o <<= 1) {
+            const u64 vn = __shfl_down_sync(FULL, v, o);
+            const u32 pn = __shfl_down_sync(FULL, par, o);
+            if (lane + o < 32 && pn == par) v += vn;
+        }
+        if (valid && (lane == 0 || prev != par)) atomicAdd(&parent_acc[par], v);
     }
-    if (stores) atomicAdd(&counters[2], stores);
+    block_count_add(&counters[2], stores);
 }
 
 // level 0: remember each slot's root, make each slot its own group
@@ -182,7 +225,7 @@ static __global__ void k_tt_roots(LevelView lv, u32 n, u32* __restrict__ root_of
 static __global__ void k_tt_finish(LevelView lv, u32 n, LevelTT lt, TTSet tt, const u32* __restrict__ root_of,
                                    u64* __restrict__ out, u64* counters)
 {
-    u64 stores = 0;
+    u32 stores = 0;
     for (u32 s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         const u32 d = lt.dup[s];
         const u64 v = d != NO_DUP ? lt.acc[d] : lt.acc[s];
@@ -193,7 +236,7 @@ static __global__ void k_tt_finish(LevelView lv, u32 n, LevelTT lt, TTSet tt, co
         }
         out[root_of[s]] = v;
     }
-    if (stores) atomicAdd(&counters[2], stores);
+    block_count_add(&counters[2], stores);
 }
 
 // ---------------------------------------------------------------------------
