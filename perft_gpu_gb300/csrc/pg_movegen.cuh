@@ -563,8 +563,10 @@ template <class E> __device__ __forceinline__ void emit_pawn(E& emit, int from, 
 // for the kernels that only need the set of children (the leaf and the level
 // expansion): king, knights, bishop/queen, rook/queen, pawn pushes, double
 // pushes, captures, castles, en passant.  Same analysis as the count, so the
-// number emitted equals the count for every position; the flags are the
-// reference's (double push, castles, en passant, promotions, captures).
+// number emitted equals the count for every position.  The flags are the
+// reference's where making the move reads them (double push, castles, en
+// passant, promotions); captures carry no flag (makeMove clears the target
+// square whatever the flag).
 // Non-pawn moves also pass the moving piece (PC_*) to the emitter.
 enum : u32 { PC_PAWN = 0, PC_KNIGHT = 1, PC_BISHOP = 2, PC_ROOK = 3, PC_QUEEN = 4, PC_KING = 5 };
 template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b, E& emit)
@@ -573,12 +575,12 @@ template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b,
     const u64 tgt = f.tgt;
     const int ksq = f.ksq;
     for (u64 m = __ldg(&g_king[ksq]) & ~(f.threat | f.mine); m; m &= m - 1)
-        emit(cmove(ksq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0), PC_KING);
+        emit(cmove(ksq, lsb(m), 0), PC_KING);
     const u64 pin_chk = f.pinned & f.chk_all;
     for (u64 s = b.n & f.mine & ~f.pinned; s; s &= s - 1) {
         const int sq = lsb(s);
         for (u64 m = __ldg(&g_knight[sq]) & tgt; m; m &= m - 1)
-            emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0), PC_KNIGHT);
+            emit(cmove(sq, lsb(m), 0), PC_KNIGHT);
     }
     // a pinned slider keeps the moves along its pin line (none if the line is
     // not its kind); in check pinned pieces do not move
@@ -588,7 +590,7 @@ template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b,
         u64 m = SlFancy::bishop(sq, f.occ) & tgt;
         if (f.pinned & bit) m &= (f.pd & bit) ? diag_of(ksq) : (f.pa & bit) ? anti_of(ksq) : 0ull;
         const u32 pc = (b.rq & bit) ? PC_QUEEN : PC_BISHOP;
-        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0), pc);
+        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), 0), pc);
     }
     for (u64 s = b.rq & f.mine & ~pin_chk; s; s &= s - 1) {
         const int sq = lsb(s);
@@ -596,7 +598,7 @@ template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b,
         u64 m = SlFancy::rook(sq, f.occ) & tgt;
         if (f.pinned & bit) m &= (f.pf & bit) ? file_of(ksq) : (f.pr & bit) ? rank_of(ksq) : 0ull;
         const u32 pc = (b.bq & bit) ? PC_QUEEN : PC_ROOK;
-        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), (lowbit(m) & f.theirs) ? MF_CAPTURE : 0), pc);
+        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), 0), pc);
     }
     // pawns, set-wise as in the count; from = to - step
     constexpr int PUSH = S ? -8 : 8, CW = S ? -9 : 7, CE = S ? -7 : 9;
@@ -608,9 +610,9 @@ template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b,
     for (u64 m = push1<S>(d1 & double_rank<S>() & ~f.safe) & f.empty & tgt; m; m &= m - 1)
         emit(cmove(lsb(m) - 2 * PUSH, lsb(m), MF_DOUBLE));
     for (u64 m = cap_w<S>(fp | (myp & (S ? f.pd : f.pa) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
-        emit_pawn(emit, lsb(m) - CW, lowbit(m), MF_CAPTURE);
+        emit_pawn(emit, lsb(m) - CW, lowbit(m), 0);
     for (u64 m = cap_e<S>(fp | (myp & (S ? f.pa : f.pd) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
-        emit_pawn(emit, lsb(m) - CE, lowbit(m), MF_CAPTURE);
+        emit_pawn(emit, lsb(m) - CE, lowbit(m), 0);
     if (!f.checkers) {
         if (can_castle_k<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 62 : 6, MF_KCASTLE), PC_KING);
         if (can_castle_q<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 58 : 2, MF_QCASTLE), PC_KING);
