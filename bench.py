@@ -261,6 +261,29 @@ def serve_leg(pg, rates, seconds, plain_rate):
         out["rates"].append({"rate_req_s": rate, "requests": n, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
                              "max_ms": max(lat) if lat else None, "leaves_per_s": leaves / wall,
                              "completed_per_s": n / wall})
+    # the same kind of stream at the middle rate, served through the
+    # transposition tables (they persist across requests)
+    arrivals = np.cumsum(rng.exponential(1.0 / plain_rate, max_n))
+    n = int(np.searchsorted(arrivals, seconds))
+    pg.tt_clear()
+    srv = pg.Server(hbm_budget_bytes=8 << 30, use_tt=True)
+    ids = []
+    t0 = time.perf_counter()
+    for i in range(n):
+        dt = t0 + arrivals[i] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        ids.append(srv.submit(pg.board_of(boards[i]), int(depths[i])))
+    res = [srv.wait(r, timeout=900) for r in ids]
+    wall = time.perf_counter() - t0
+    srv.stop()
+    lat = [l for _, l in res]
+    ref = pg.perft_batch(boards[:n], depths[:n])
+    assert [int(r) for r, _ in res] == [int(x) for x in ref], "TT-served counts differ"
+    check_n += n
+    out["tt"] = {"rate_req_s": plain_rate, "requests": n, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+                 "max_ms": max(lat) if lat else None, "leaves_per_s": sum(int(r) for r, _ in res) / wall,
+                 "path": "server with use_tt (tables persist across requests)"}
     # plain: one engine call per request, FIFO, same kind of stream
     arrivals = np.cumsum(rng.exponential(1.0 / plain_rate, max_n))
     n = int(np.searchsorted(arrivals, seconds))

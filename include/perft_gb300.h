@@ -208,6 +208,9 @@ typedef struct pg_server_config {
     uint32_t max_inflight;       /* request slots; 0 = 4096 */
     int slider;
     uint32_t max_wave_nodes;     /* frontier nodes the scheduler advances per wave; 0 = auto */
+    int use_tt;                  /* count the waves through the transposition tables, which persist
+                                    across requests (launcher.h:699-790 keeps its table across runs) */
+    uint64_t tt_bytes;           /* TT size when use_tt; 0 = from the engine budget (as pg_opts) */
 } pg_server_config;
 
 int pg_server_start(const pg_server_config *cfg);

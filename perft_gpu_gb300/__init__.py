@@ -125,7 +125,8 @@ class PgTuning(ctypes.Structure):
 
 class PgServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
-                ("slider", ctypes.c_int), ("max_wave_nodes", ctypes.c_uint32)]
+                ("slider", ctypes.c_int), ("max_wave_nodes", ctypes.c_uint32),
+                ("use_tt", ctypes.c_int), ("tt_bytes", ctypes.c_uint64)]
 
 
 _BP = ctypes.POINTER(HexaBitBoardPosition)
@@ -361,9 +362,10 @@ class Server:
     """Continuous-batching perft server (pg_server_*)."""
 
     def __init__(self, hbm_budget_bytes: int = 0, max_inflight: int = 0, slider: int | str = 0,
-                 max_wave_nodes: int = 0):
+                 max_wave_nodes: int = 0, use_tt: bool = False, tt_bytes: int = 0):
         cfg = PgServerConfig(hbm_budget_bytes, max_inflight,
-                             SLIDERS[slider] if isinstance(slider, str) else slider, max_wave_nodes)
+                             SLIDERS[slider] if isinstance(slider, str) else slider, max_wave_nodes,
+                             1 if use_tt else 0, tt_bytes)
         _check(load_library().pg_server_start(ctypes.byref(cfg)))
 
     def submit(self, pos: HexaBitBoardPosition, depth: int) -> int:

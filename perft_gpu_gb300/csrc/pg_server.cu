@@ -31,6 +31,7 @@
 
 #include "pg_engine.cuh"
 #include "pg_level.cuh"
+#include "pg_tt.cuh"
 
 namespace pg {
 namespace {
@@ -59,6 +60,34 @@ __global__ void k_gather_wave(const Pos* __restrict__ pool, const Segment* __res
         out[i] = pool[s.src + (i - s.dst)];
         dep[i] = (unsigned char)s.depth;
         grp[i] = s.group;
+    }
+}
+
+// TT waves: add each task's count into its request's counter.  A request's
+// tasks form runs of adjacent wave slots (one run per segment); a warp numbers
+// the runs among its lanes, sums each run with a segmented shuffle reduction
+// and adds it with one atomic.
+__global__ void k_add_groups(const u64* __restrict__ task_out, const u32* __restrict__ grp, u32 total,
+                             u64* __restrict__ acc)
+{
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    const u32 lane = threadIdx.x & 31;
+    const u32 stride = gridDim.x * blockDim.x;  // a multiple of 32
+    for (u32 base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < total; base += stride) {
+        const u32 i = base + lane;
+        const bool valid = i < total;
+        const u32 g = valid ? grp[i] : 0xFFFFFFFFu;
+        u64 v = valid ? task_out[i] : 0;
+        const u32 prev = __shfl_up_sync(FULL, g, 1);
+        const bool head = lane == 0 || prev != g;
+        const u32 heads = __ballot_sync(FULL, head);
+        const u32 run = __popc(heads & (0xFFFFFFFFu >> (31 - lane)));  // runs up to and including this lane
+        for (u32 o = 1; o < 32; o <<= 1) {
+            const u64 vn = __shfl_down_sync(FULL, v, o);
+            const u32 rn = __shfl_down_sync(FULL, run, o);
+            if (lane + o < 32 && rn == run) v += vn;
+        }
+        if (valid && head) atomicAdd(&acc[g], v);
     }
 }
 
@@ -131,6 +160,8 @@ struct Server {
     std::vector<int> free_slots;
     u32 max_inflight = 4096;
     int slider = 0;
+    bool use_tt = false;
+    u64 tt_bytes = 0;
     double wave_leaves = 4e9;
     // device
     u64* acc = nullptr;
@@ -140,6 +171,7 @@ struct Server {
     Pos* wave_pos = nullptr;
     unsigned char* wave_dep = nullptr;
     u32* wave_grp = nullptr;
+    u64* task_out = nullptr;      // per-task counts of a TT wave
     Segment* seg_dev = nullptr;
     Segment* seg_host = nullptr;  // pinned
     u64* acc_host = nullptr;      // pinned
@@ -261,7 +293,19 @@ int run_wave(Server& S, std::unique_lock<std::mutex>& lk)
     cudaMemsetAsync(E.err, 0, sizeof(u32), E.stream);
     pg_opts o{};
     o.slider = S.slider;
-    int st = perft_core(S.wave_pos, S.wave_dep, S.wave_grp, total, S.acc, false, pick_variant(&o));
+    int st;
+    if (S.use_tt) {
+        o.use_tt = 1;
+        o.tt_bytes = S.tt_bytes;
+        st = tt_perft_batch_device(S.wave_pos, S.wave_dep, total, S.task_out, &o);
+        if (st == PG_OK) {
+            k_add_groups<<<std::min<u32>((total + 255) / 256, 2048), 256, 0, E.stream>>>(S.task_out, S.wave_grp,
+                                                                                       total, S.acc);
+            if (cudaGetLastError() != cudaSuccess) st = PG_ERR_CUDA;
+        }
+    } else {
+        st = perft_core(S.wave_pos, S.wave_dep, S.wave_grp, total, S.acc, false, pick_variant(&o));
+    }
     if (st == PG_OK) {
         if (cudaMemcpyAsync(S.acc_host, S.acc, S.max_inflight * sizeof(u64), cudaMemcpyDeviceToHost, E.stream) !=
                 cudaSuccess ||
@@ -317,6 +361,7 @@ void release(Server* S)
     if (S->wave_pos) cudaFree(S->wave_pos);
     if (S->wave_dep) cudaFree(S->wave_dep);
     if (S->wave_grp) cudaFree(S->wave_grp);
+    if (S->task_out) cudaFree(S->task_out);
     if (S->seg_dev) cudaFree(S->seg_dev);
     if (S->seg_host) cudaFreeHost(S->seg_host);
     if (S->acc_host) cudaFreeHost(S->acc_host);
@@ -347,6 +392,8 @@ int pg_server_start(const pg_server_config* cfg)
     Server* S = new Server();
     S->max_inflight = (cfg && cfg->max_inflight) ? cfg->max_inflight : 4096;
     S->slider = cfg ? cfg->slider : 0;
+    S->use_tt = cfg && cfg->use_tt;
+    S->tt_bytes = cfg ? cfg->tt_bytes : 0;
     if (cfg && cfg->max_wave_nodes) S->wave_leaves = (double)cfg->max_wave_nodes * est_leaves(TASK_DEPTH);
     const u64 budget = (cfg && cfg->hbm_budget_bytes) ? cfg->hbm_budget_bytes : (2ull << 30);
     S->pool_cap = budget / sizeof(Pos);
@@ -357,6 +404,7 @@ int pg_server_start(const pg_server_config* cfg)
     if (e == cudaSuccess) e = cudaMalloc(&S->wave_pos, MAX_WAVE_TASKS * sizeof(Pos));
     if (e == cudaSuccess) e = cudaMalloc(&S->wave_dep, MAX_WAVE_TASKS);
     if (e == cudaSuccess) e = cudaMalloc(&S->wave_grp, MAX_WAVE_TASKS * sizeof(u32));
+    if (e == cudaSuccess && S->use_tt) e = cudaMalloc(&S->task_out, MAX_WAVE_TASKS * sizeof(u64));
     if (e == cudaSuccess) e = cudaMalloc(&S->seg_dev, (S->max_inflight * 2 + 8) * sizeof(Segment));
     if (e == cudaSuccess) e = cudaMallocHost(&S->seg_host, (S->max_inflight * 2 + 8) * sizeof(Segment));
     if (e == cudaSuccess) e = cudaMallocHost(&S->acc_host, S->max_inflight * sizeof(u64));

@@ -53,3 +53,26 @@ def test_server_rejects_invalid_and_reports_latency(pg):
         srv.stop()
     assert [r for r, _ in res] == [20, 400, 8902, 197281, 4865609, 119060324, 1]
     assert all(lat >= 0 for _, lat in res)
+
+
+def test_server_with_tt_matches_golden_and_repeats(pg):
+    """Served through the transposition tables: each count equals the golden
+    count; the same requests submitted again (the tables now hold their
+    subtrees) give the same counts."""
+    g3 = golden_npz("config3.npz")
+    g2 = golden_json("config2.json")
+    deep = pg.HexaBitBoardPosition(*words_of_hex(g2["board"]))
+    idx = np.arange(7, 4096, 53)
+    boards = g3["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    pg.tt_clear()
+    srv = pg.Server(hbm_budget_bytes=1 << 30, max_inflight=256, use_tt=True, tt_bytes=1 << 30)
+    try:
+        for _ in range(2):
+            want = {srv.submit(deep, 7): g2["perft7"]}
+            for k, i in enumerate(idx):
+                want[srv.submit(pg.board_of(boards[k]), int(g3["depths"][i]))] = int(g3["totals"][i])
+            got = {rid: srv.wait(rid, timeout=300)[0] for rid in want}
+            assert got == want
+    finally:
+        srv.stop()
+        pg.tt_clear()
