@@ -84,3 +84,17 @@ def test_cli_records_mode_resumes(tmp_path):
     for k, (n, line) in enumerate(zip(names, lines)):
         res, weighted = line.split()[-2:]
         assert int(res) == fens[n]["perft"]["4"] and int(weighted) == fens[n]["perft"]["4"] * (k + 1)
+
+
+def test_python_cli_tt_options(tmp_path):
+    """python -m perft_gpu_gb300 with a small TT, a capped HBM budget and the
+    engine counters: same counts as the reference, counters printed."""
+    import sys
+    fens = {f["name"]: f for f in golden_json("fens.json")}
+    cmd = [sys.executable, "-m", "perft_gpu_gb300", fens["position3"]["fen"], "5", "--min-depth", "4",
+           "--tt", "--tt-mib", "64", "--hbm-budget-mib", "1024", "--stats"]
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert out.returncode == 0, out.stderr
+    assert "GPU Perft 4: %d," % fens["position3"]["perft"]["4"] in out.stdout
+    assert "GPU Perft 5: %d," % fens["position3"]["perft"]["5"] in out.stdout
+    assert "tt_probes=" in out.stdout and "tt_stores=" in out.stdout
