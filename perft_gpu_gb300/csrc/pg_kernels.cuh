@@ -266,24 +266,33 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
         const u64 i = c0 + tid;
         Pos b{0, 0, 0, 0, 0, 0};
         u32 grp = 0, c = 0;
+        // the Kogge-Stone and hybrid policies count the node from the same
+        // analysis the generator uses: made once, kept across the block scan
+        constexpr bool kFacts = SL::kId == 0 || SL::kId == 3;
+        KsFacts<S> f{};
         if (i < n) {
             b = load_board(lv, start + i);
             grp = lv.grp[start + i];
             const int rem = lv.rem[start + i];
-            if (rem == 2 && max_rem >= 2) c = count_moves<S, SL>(b);
-            else if (rem == 1) ga.add(acc, grp, count_moves<S, SL>(b));
-            else if (rem == 0) ga.add(acc, grp, 1);
+            if (rem == 2 && max_rem >= 2) {
+                if constexpr (kFacts) {
+                    f = ks_facts<S>(b);
+                    c = count_from_facts<S, SL::kId == 3>(b, f);
+                } else {
+                    c = count_moves<S, SL>(b);
+                }
+            } else if (rem == 1) {
+                ga.add(acc, grp, count_moves<S, SL>(b));
+            } else if (rem == 0) {
+                ga.add(acc, grp, 1);
+            }
         }
         sb[tid] = b;
         sg[tid] = grp;
         u32 total;
         const u32 off = block_excl_scan<T>(c, total, s_warp);
-        for (u32 lo = 0; lo < total; lo += QCAP) {
-            const u32 hi = min(lo + (u32)QCAP, total);
-            if (c && off < hi && off + c > lo) {
-                QEmit e{q, off, lo, hi, (u32)tid << 16};
-                gen_leaf<S>(b, e);
-            }
+        // make and count the queued children of window [lo, hi)
+        auto children = [&](u32 lo, u32 hi) {
             __syncthreads();
             const u32 m = hi - lo;
             for (u32 e = tid; e < m; e += T) {
@@ -294,6 +303,25 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
                 ga.add(acc, sg[p], count_moves<1 - S, SL>(ch));
             }
             __syncthreads();
+        };
+        // the first window generates from the kept analysis; later ones (rare:
+        // more children than the queue holds) make it again
+        if (total) {
+            const u32 hi = min((u32)QCAP, total);
+            if (c && off < hi) {
+                QEmit e{q, off, 0u, hi, (u32)tid << 16};
+                if constexpr (kFacts) gen_from_facts<S>(b, f, e);
+                else gen_leaf<S>(b, e);
+            }
+            children(0u, hi);
+        }
+        for (u32 lo = QCAP; lo < total; lo += QCAP) {
+            const u32 hi = min(lo + (u32)QCAP, total);
+            if (c && off < hi && off + c > lo) {
+                QEmit e{q, off, lo, hi, (u32)tid << 16};
+                gen_leaf<S>(b, e);
+            }
+            children(lo, hi);
         }
     }
     ga.flush_warp(acc);

@@ -372,9 +372,8 @@ template <int S> __device__ __forceinline__ KsFacts<S> ks_facts(const Pos& b)
 // reference's in every case (proved per term in the comments of the
 // reference-shaped paths above and checked bit-exact by the tests).
 template <int S, bool OWN_BY_LOOKUP = false>
-__device__ __forceinline__ u32 count_moves_ks(const Pos& b)
+__device__ __forceinline__ u32 count_from_facts(const Pos& b, const KsFacts<S>& f)
 {
-    const KsFacts<S> f = ks_facts<S>(b);
     const u64 pawns = f.pawns, occ = f.occ, mine = f.mine, theirs = f.theirs, empty = f.empty;
     const u64 pf = f.pf, pr = f.pr, pd = f.pd, pa = f.pa, pinned = f.pinned, checkers = f.checkers;
     const u64 safe = f.safe, threat = f.threat, chk_all = f.chk_all, tgt = f.tgt;
@@ -446,6 +445,12 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     if (!in_check) n += can_castle_k<S>(b, occ, threat) + can_castle_q<S>(b, occ, threat);
     if (b.p & 0xF0ull) n += count_ep_ks<S>(b, pinned, checkers);
     return n;
+}
+
+template <int S, bool OWN_BY_LOOKUP = false>
+__device__ __forceinline__ u32 count_moves_ks(const Pos& b)
+{
+    return count_from_facts<S, OWN_BY_LOOKUP>(b, ks_facts<S>(b));
 }
 
 // countMoves / countMovesOutOfCheck (MGB.h:3008-3295, 2825-3002) for the
@@ -569,9 +574,8 @@ template <class E> __device__ __forceinline__ void emit_pawn(E& emit, int from, 
 // square whatever the flag).
 // Non-pawn moves also pass the moving piece (PC_*) to the emitter.
 enum : u32 { PC_PAWN = 0, PC_KNIGHT = 1, PC_BISHOP = 2, PC_ROOK = 3, PC_QUEEN = 4, PC_KING = 5 };
-template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b, E& emit)
+template <int S, class E> __device__ __forceinline__ void gen_from_facts(const Pos& b, const KsFacts<S>& f, E& emit)
 {
-    const KsFacts<S> f = ks_facts<S>(b);
     const u64 tgt = f.tgt;
     const int ksq = f.ksq;
     for (u64 m = __ldg(&g_king[ksq]) & ~(f.threat | f.mine); m; m &= m - 1)
@@ -632,6 +636,11 @@ template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b,
                 if (ep_legal<S>(c, f.pinned, lowbit(cand), et, victim)) emit(cmove(lsb(cand), to, MF_EP));
         }
     }
+}
+
+template <int S, class E> __device__ __forceinline__ void gen_leaf(const Pos& b, E& emit)
+{
+    gen_from_facts<S>(b, ks_facts<S>(b), emit);
 }
 
 // generateMovesOutOfCheck (MGB.h:2266-2463)
