@@ -402,9 +402,10 @@ __device__ __forceinline__ u32 count_from_facts(const Pos& b, const KsFacts<S>& 
             n += popc(m);
         }
     } else {
-        // pass 2: own slider moves.  The propagator chains are rebuilt from an
-        // opaque copy of `empty` so the compiler does not keep pass 1's chains
-        // alive (a few more ALU operations for far fewer live registers).
+        // pass 2: own slider moves, through the real empty squares (pass 1's
+        // chains treat the king as empty).  The chains are built from an
+        // opaque copy of `empty`, so the compiler builds them here rather than
+        // early, where they would be live across pass 1.
         u64 empty2 = empty;
         asm volatile("" : "+l"(empty2));
         {
