@@ -9,11 +9,14 @@
 namespace pg {
 namespace {
 
-// shared-memory queue entries per CTA: 32 per thread leaves room for the
-// ~35 average children of a middlegame node in one round; the byte-lookup
-// policy gives 158 KB of the CTA's shared memory to its tables and keeps 8
+// shared-memory queue entries per CTA: 64 per thread hold the children of
+// a CTA's nodes in one window even for positions with ~50 moves (the leaf
+// kernel's first window generates from the count's analysis; a second
+// window makes it again and runs a second copy of the hot loop); the
+// byte-lookup policy gives 158 KB of the CTA's shared memory to its tables
+// and keeps 8
 template <class SL, int T> struct QcapFor {
-    static constexpr int value = SL::kId == 2 ? T * 8 : T * 32;
+    static constexpr int value = SL::kId == 2 ? T * 8 : T * 64;
 };
 
 inline int occupancy_grid(const void* fn, int T, int smem, u64 items, int num_sms)
