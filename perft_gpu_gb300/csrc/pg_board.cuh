@@ -54,6 +54,8 @@ __host__ __device__ __forceinline__ u16 cmove(int from, int to, int fl)
 }
 
 __device__ __forceinline__ int lsb(u64 x) { return __ffsll((long long)x) - 1; }
+// the square of a one-bit set (count of leading zeros; 63 for an empty set)
+__device__ __forceinline__ int sq_of(u64 one) { return (63 - __clzll((long long)one)) & 63; }
 __device__ __forceinline__ int popc(u64 x) { return __popcll(x); }
 __device__ __forceinline__ u64 lowbit(u64 x) { return x & (0ull - x); }
 __device__ __forceinline__ bool several(u64 x) { return (x & (x - 1)) != 0; }
@@ -140,6 +142,22 @@ __device__ __forceinline__ u64 ks_bishop(u64 g, u64 empty)
 {
     return ray<9, true>(g, empty) | ray<7, true>(g, empty) | ray<7, false>(g, empty) | ray<9, false>(g, empty);
 }
+// both vertical fills at once: with no wrap mask the down chain is the up
+// chain shifted (p2 down = p2 up >> 8, p4 down = p4 up >> 24)
+__device__ __forceinline__ void vertical_fills(u64 empty, u64 g, u64& up_att, u64& down_att)
+{
+    const u64 p2 = empty & (empty << 8), p4 = p2 & (p2 << 16);
+    const u64 q2 = p2 >> 8, q4 = p4 >> 24;
+    u64 a = g | (empty & (g << 8));
+    a |= p2 & (a << 16);
+    a |= p4 & (a << 32);
+    up_att = a << 8;
+    u64 c = g | (empty & (g >> 8));
+    c |= q2 & (c >> 16);
+    c |= q4 & (c >> 32);
+    down_att = c >> 8;
+}
+
 __device__ __forceinline__ u64 ks_rook(u64 g, u64 empty)
 {
     return ray<8, true>(g, empty) | ray<8, false>(g, empty) | ray<1, true>(g, empty) | ray<1, false>(g, empty);

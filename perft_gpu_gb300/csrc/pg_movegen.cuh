@@ -39,6 +39,7 @@ static __device__ __align__(16) unsigned char g_magic_bytes[MAGIC_TABLE_ENTRIES]
 static __device__ u64 g_magic_unique[UNIQUE_TOTAL];
 static __device__ u64 g_knight[64];
 static __device__ u64 g_king[64];
+static __device__ u64 g_diag[64];
 
 // uploads this translation unit's copy of the tables
 static inline cudaError_t upload_static_tables(const HostTables& t)
@@ -50,6 +51,7 @@ static inline cudaError_t upload_static_tables(const HostTables& t)
     if ((e = cudaMemcpyToSymbol(g_magic_bytes, t.bytes.data(), t.bytes.size()))) return e;
     if ((e = cudaMemcpyToSymbol(g_magic_unique, t.unique.data(), t.unique.size() * sizeof(u64)))) return e;
     if ((e = cudaMemcpyToSymbol(g_king, t.king, sizeof(t.king)))) return e;
+    if ((e = cudaMemcpyToSymbol(g_diag, t.diag, sizeof(t.diag)))) return e;
     return cudaMemcpyToSymbol(g_knight, t.knight, sizeof(t.knight));
 }
 
@@ -316,14 +318,16 @@ template <int S> __device__ __forceinline__ KsFacts<S> ks_facts(const Pos& b)
     // enemy slider fills per line kind, with the king taken off the board so
     // that the squares behind it on a checking line are attacked
     const u64 et = empty | king;
-    const u64 a_v = line_fill<8>(et, trq), a_h = line_fill<1>(et, trq);
+    u64 a_up, a_dn;
+    vertical_fills(et, trq, a_up, a_dn);
+    const u64 a_v = a_up | a_dn, a_h = line_fill<1>(et, trq);
     const u64 a_d = line_fill<9>(et, tbq), a_a = line_fill<7>(et, tbq);
 
     // the king's rays (first blockers included): one rook and one bishop
     // lookup, split into the four lines
-    const int ksq = lsb(king) & 63;
+    const int ksq = sq_of(king);
     const u64 kr = SlFancy::rook(ksq, occ), kb = SlFancy::bishop(ksq, occ);
-    const u64 kf = kr & file_of(ksq), kd = kb & diag_of(ksq);
+    const u64 kf = kr & file_of(ksq), kd = kb & __ldg(&g_diag[ksq]);
     const u64 kh = kr ^ kf, ka = kb ^ kd;
 
     // A first blocker of the king on a line is pinned when an enemy slider
@@ -351,7 +355,7 @@ template <int S> __device__ __forceinline__ KsFacts<S> ks_facts(const Pos& b)
     const int csq = lsb(csl) & 63;
     const u64 cray = SlFancy::look(cr ? g_magic_rook : g_magic_bishop, csq, occ) & (cr ? kr : kb);
     f.safe = (csl ? cray : 0ull) | f.checkers;
-    f.threat = a_v | a_h | a_d | a_a | pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[lsb(b.k & theirs) & 63]);
+    f.threat = a_v | a_h | a_d | a_a | pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[sq_of(b.k & theirs)]);
     const bool in_check = f.checkers != 0;
     f.chk_all = in_check ? ~0ull : 0ull;
     f.tgt = several(f.checkers) ? 0ull : (in_check ? f.safe : ~mine);
@@ -410,7 +414,9 @@ __device__ __forceinline__ u32 count_from_facts(const Pos& b, const KsFacts<S>& 
         asm volatile("" : "+l"(empty2));
         {
             const u64 ns = my_rq & ~((pinned ^ pf) | pin_chk);
-            n += popc(Pro<8, true>(empty2).attacks(ns) & tgt) + popc(Pro<8, false>(empty2).attacks(ns) & tgt);
+            u64 up_att, down_att;
+            vertical_fills(empty2, ns, up_att, down_att);
+            n += popc(up_att & tgt) + popc(down_att & tgt);
         }
         {
             const u64 ew = my_rq & ~((pinned ^ pr) | pin_chk);
@@ -476,7 +482,7 @@ __device__ __forceinline__ u32 count_moves_mg(const Pos& b)
     const u64 trq = b.rq & theirs, tbq = b.bq & theirs;
     const u64 tp = pawns & theirs, tn = b.n & theirs;
 
-    u64 threat = pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[lsb(b.k & theirs) & 63]);
+    u64 threat = pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[sq_of(b.k & theirs)]);
     for (u64 s = trq; s; s &= s - 1) threat |= SL::rook(lsb(s), occ);
     for (u64 s = tbq; s; s &= s - 1) threat |= SL::bishop(lsb(s), occ);
 

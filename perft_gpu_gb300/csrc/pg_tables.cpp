@@ -126,6 +126,8 @@ int build_tables(HostTables& t)
         const u64 row = b | a;
         t.king[s] = ((b >> 1) & ~(0x0101010101010101ull << 7)) | ((b << 1) & ~0x0101010101010101ull) | (row << 8) |
                     (row >> 8);
+        const int d = (s >> 3) - (s & 7);
+        t.diag[s] = d >= 0 ? (0x8040201008040201ull << (8 * d)) : (0x8040201008040201ull >> (-8 * d));
     }
     return 0;
 }

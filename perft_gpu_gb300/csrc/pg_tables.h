@@ -26,6 +26,7 @@ struct HostTables {
     std::vector<u64> unique;
     u64 knight[64];
     u64 king[64];
+    u64 diag[64];  // the a1-h8 diagonal through each square
 };
 
 // built once per process; nullptr if the search failed
