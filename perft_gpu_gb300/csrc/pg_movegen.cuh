@@ -40,6 +40,7 @@ static __device__ u64 g_magic_unique[UNIQUE_TOTAL];
 static __device__ u64 g_knight[64];
 static __device__ u64 g_king[64];
 static __device__ u64 g_diag[64];
+static __device__ u64 g_pawn_checks[2][64];
 
 // uploads this translation unit's copy of the tables
 static inline cudaError_t upload_static_tables(const HostTables& t)
@@ -52,6 +53,7 @@ static inline cudaError_t upload_static_tables(const HostTables& t)
     if ((e = cudaMemcpyToSymbol(g_magic_unique, t.unique.data(), t.unique.size() * sizeof(u64)))) return e;
     if ((e = cudaMemcpyToSymbol(g_king, t.king, sizeof(t.king)))) return e;
     if ((e = cudaMemcpyToSymbol(g_diag, t.diag, sizeof(t.diag)))) return e;
+    if ((e = cudaMemcpyToSymbol(g_pawn_checks, t.pawn_checks, sizeof(t.pawn_checks)))) return e;
     return cudaMemcpyToSymbol(g_knight, t.knight, sizeof(t.knight));
 }
 
@@ -344,16 +346,18 @@ template <int S> __device__ __forceinline__ KsFacts<S> ks_facts(const Pos& b)
     f.pinned = f.pf | f.pr | f.pd | f.pa;
     const u64 cr = kr & trq, cb = kb & tbq;
     const u64 nchk = __ldg(&g_knight[ksq]) & tn;
-    const u64 pchk = pawn_attackers_of<S>(king) & tp;
+    const u64 pchk = __ldg(&g_pawn_checks[S][ksq]) & tp;
     const u64 csl = cr | cb;
     f.checkers = csl | nchk | pchk;
     // single slider check: the squares between the king and the checker are
     // where the king's rays meet the checker's rays of the same kind (the
-    // other lines of the two pieces are parallel); looked up unconditionally
-    // (a warp rarely agrees on being out of check) and dropped when no slider
-    // checks
+    // other lines of the two pieces are parallel); looked up by every lane
+    // when any lane of the warp has a slider checker (no divergence), and
+    // dropped where no slider checks
     const int csq = lsb(csl) & 63;
-    const u64 cray = SlFancy::look(cr ? g_magic_rook : g_magic_bishop, csq, occ) & (cr ? kr : kb);
+    u64 cray = 0;
+    if (__any_sync(__activemask(), csl != 0))
+        cray = SlFancy::look(cr ? g_magic_rook : g_magic_bishop, csq, occ) & (cr ? kr : kb);
     f.safe = (csl ? cray : 0ull) | f.checkers;
     f.threat = a_v | a_h | a_d | a_a | pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[sq_of(b.k & theirs)]);
     const bool in_check = f.checkers != 0;

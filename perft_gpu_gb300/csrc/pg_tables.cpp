@@ -128,6 +128,9 @@ int build_tables(HostTables& t)
                     (row >> 8);
         const int d = (s >> 3) - (s & 7);
         t.diag[s] = d >= 0 ? (0x8040201008040201ull << (8 * d)) : (0x8040201008040201ull >> (-8 * d));
+        const u64 not_a = ~0x0101010101010101ull, not_h = ~0x8080808080808080ull;
+        t.pawn_checks[0][s] = ((b << 9) & not_a) | ((b << 7) & not_h);  // black pawns above a white king
+        t.pawn_checks[1][s] = ((b >> 7) & not_a) | ((b >> 9) & not_h);  // white pawns below a black king
     }
     return 0;
 }

@@ -27,6 +27,7 @@ struct HostTables {
     u64 knight[64];
     u64 king[64];
     u64 diag[64];  // the a1-h8 diagonal through each square
+    u64 pawn_checks[2][64];  // squares from which an enemy pawn attacks a king of side s on square q
 };
 
 // built once per process; nullptr if the search failed
