@@ -93,7 +93,7 @@ struct QEmit {
         if (pos >= lo && pos < hi) q[pos - lo] = tag | m;
         ++pos;
     }
-    // bits 25-27 carry the moving piece (PC_*) for make_child
+    // bits 25-28 carry the moving piece (PC_*) and PC_EP_FLAG for make_child
     __device__ __forceinline__ void operator()(u16 m, u32 piece)
     {
         if (pos >= lo && pos < hi) q[pos - lo] = tag | m | (piece << 25);
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
                 const u32 ent = q[e];
                 const u32 p = (ent >> 16) & (T - 1);  // in bounds even if a queue slot was left unwritten
                 Pos ch = sb[p];
-                make_child<S>(ch, (u16)(ent & 0xFFFFu), (ent >> 25) & 7u);
+                make_child<S>(ch, (u16)(ent & 0xFFFFu), (ent >> 25) & 15u);
                 ga.add(acc, sg[p], count_moves<1 - S, SL>(ch));
             }
             __syncthreads();

@@ -585,6 +585,9 @@ template <class E> __device__ __forceinline__ void emit_pawn(E& emit, int from, 
 // square whatever the flag).
 // Non-pawn moves also pass the moving piece (PC_*) to the emitter.
 enum : u32 { PC_PAWN = 0, PC_KNIGHT = 1, PC_BISHOP = 2, PC_ROOK = 3, PC_QUEEN = 4, PC_KING = 5 };
+// with a double push: an enemy pawn stands beside the pushed pawn, so the
+// child's en-passant file is set (exact flagging, decided by the parent)
+constexpr u32 PC_EP_FLAG = 8;
 template <int S, class E> __device__ __forceinline__ void gen_from_facts(const Pos& b, const KsFacts<S>& f, E& emit)
 {
     const u64 tgt = f.tgt;
@@ -622,8 +625,12 @@ template <int S, class E> __device__ __forceinline__ void gen_from_facts(const P
     const u64 pin_ok = ~f.chk_all;
     const u64 d1 = push1<S>(fp | (myp & f.pf & pin_ok)) & f.empty;
     for (u64 m = d1 & tgt; m; m &= m - 1) emit_pawn(emit, lsb(m) - PUSH, lowbit(m), 0);
-    for (u64 m = push1<S>(d1 & double_rank<S>() & ~f.safe) & f.empty & tgt; m; m &= m - 1)
-        emit(cmove(lsb(m) - 2 * PUSH, lsb(m), MF_DOUBLE));
+    const u64 their_pawns = f.pawns & f.theirs;
+    for (u64 m = push1<S>(d1 & double_rank<S>() & ~f.safe) & f.empty & tgt; m; m &= m - 1) {
+        const u64 t = lowbit(m);
+        emit(cmove(lsb(m) - 2 * PUSH, lsb(m), MF_DOUBLE),
+             PC_PAWN | (((east1(t) | west1(t)) & their_pawns) ? PC_EP_FLAG : 0u));
+    }
     for (u64 m = cap_w<S>(fp | (myp & (S ? f.pd : f.pa) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
         emit_pawn(emit, lsb(m) - CW, lowbit(m), 0);
     for (u64 m = cap_e<S>(fp | (myp & (S ? f.pa : f.pd) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
@@ -842,7 +849,8 @@ __device__ __forceinline__ void make_move(Pos& b, u16 mv)
 // for the side to move next reads (the pieces, that side's castling rights
 // and the exact en-passant file, as make_move) and leaves the mover's own
 // castling rights and the side bit as they were.  `piece` is the moving piece
-// (PC_*), so nothing is looked up on the board to find it.
+// (PC_*), so nothing is looked up on the board to find it, plus PC_EP_FLAG on
+// a double push that gives the opponent an en-passant capture.
 template <int S>
 __device__ __forceinline__ void make_child(Pos& b, u16 mv, u32 piece)
 {
@@ -850,16 +858,17 @@ __device__ __forceinline__ void make_child(Pos& b, u16 mv, u32 piece)
     const u64 src = 1ull << from, dst = 1ull << to;
     const bool promo = fl & 8;
     const int pr = fl & 3;  // promotion piece: 0 N, 1 B, 2 R, 3 Q
-    const bool toN = promo ? pr == 0 : piece == PC_KNIGHT;
-    const bool toB = promo ? (pr & 1) != 0 : (piece == PC_BISHOP || piece == PC_QUEEN);
-    const bool toR = promo ? pr >= 2 : (piece == PC_ROOK || piece == PC_QUEEN);
-    const bool toP = !promo && piece == PC_PAWN;
+    const u32 pc = piece & 7u;
+    const bool toN = promo ? pr == 0 : pc == PC_KNIGHT;
+    const bool toB = promo ? (pr & 1) != 0 : (pc == PC_BISHOP || pc == PC_QUEEN);
+    const bool toR = promo ? pr >= 2 : (pc == PC_ROOK || pc == PC_QUEEN);
+    const bool toP = !promo && pc == PC_PAWN;
     const u64 clr = ~(src | dst);
     b.bq = (b.bq & clr) | (toB ? dst : 0ull);
     b.rq = (b.rq & clr) | (toR ? dst : 0ull);
     b.n = (b.n & clr) | (toN ? dst : 0ull);
     b.p = (b.p & ~((src | dst) & INNER)) | (toP ? dst : 0ull);
-    if (piece == PC_KING) b.k = (b.k ^ src) | dst;
+    if (pc == PC_KING) b.k = (b.k ^ src) | dst;
     b.w = S ? (b.w & ~dst) : ((b.w ^ src) | dst);
     if (fl == MF_EP) {
         const u64 victim = S ? up(dst) : down(dst);
@@ -875,12 +884,7 @@ __device__ __forceinline__ void make_child(Pos& b, u16 mv, u32 piece)
     }
     set_ep(b, 0);
     castle_update(b, dst, S);  // a capture on the other side's rook corner
-    if (fl == MF_DOUBLE) {
-        const u64 pawns = b.p & INNER;
-        const u64 occ = b.k | pawns | b.n | b.bq | b.rq;
-        const u64 enemy = S ? b.w : (occ & ~b.w);
-        if ((east1(dst) | west1(dst)) & pawns & enemy) set_ep(b, (from & 7) + 1);
-    }
+    if (piece & PC_EP_FLAG) set_ep(b, (from & 7) + 1);
 }
 
 // ---------------------------------------------------------------------------
