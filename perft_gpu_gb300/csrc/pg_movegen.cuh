@@ -588,6 +588,21 @@ enum : u32 { PC_PAWN = 0, PC_KNIGHT = 1, PC_BISHOP = 2, PC_ROOK = 3, PC_QUEEN = 
 // with a double push: an enemy pawn stands beside the pushed pawn, so the
 // child's en-passant file is set (exact flagging, decided by the parent)
 constexpr u32 PC_EP_FLAG = 8;
+// a pawn move for the leaf: promotions N, B, Q, R (the reference's flags)
+// with the promoted piece as the landing piece
+template <class E> __device__ __forceinline__ void emit_pawn_leaf(E& emit, int from, u64 dst, int fl)
+{
+    const int to = lsb(dst);
+    if (dst & BACK_RANKS) {
+        emit(cmove(from, to, fl | MF_PROMO_N), PC_KNIGHT);
+        emit(cmove(from, to, fl | MF_PROMO_B), PC_BISHOP);
+        emit(cmove(from, to, fl | MF_PROMO_Q), PC_QUEEN);
+        emit(cmove(from, to, fl | MF_PROMO_R), PC_ROOK);
+    } else {
+        emit(cmove(from, to, fl), PC_PAWN);
+    }
+}
+
 template <int S, class E> __device__ __forceinline__ void gen_from_facts(const Pos& b, const KsFacts<S>& f, E& emit)
 {
     const u64 tgt = f.tgt;
@@ -624,7 +639,7 @@ template <int S, class E> __device__ __forceinline__ void gen_from_facts(const P
     const u64 fp = myp & ~f.pinned;
     const u64 pin_ok = ~f.chk_all;
     const u64 d1 = push1<S>(fp | (myp & f.pf & pin_ok)) & f.empty;
-    for (u64 m = d1 & tgt; m; m &= m - 1) emit_pawn(emit, lsb(m) - PUSH, lowbit(m), 0);
+    for (u64 m = d1 & tgt; m; m &= m - 1) emit_pawn_leaf(emit, lsb(m) - PUSH, lowbit(m), 0);
     const u64 their_pawns = f.pawns & f.theirs;
     for (u64 m = push1<S>(d1 & double_rank<S>() & ~f.safe) & f.empty & tgt; m; m &= m - 1) {
         const u64 t = lowbit(m);
@@ -632,9 +647,9 @@ template <int S, class E> __device__ __forceinline__ void gen_from_facts(const P
              PC_PAWN | (((east1(t) | west1(t)) & their_pawns) ? PC_EP_FLAG : 0u));
     }
     for (u64 m = cap_w<S>(fp | (myp & (S ? f.pd : f.pa) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
-        emit_pawn(emit, lsb(m) - CW, lowbit(m), 0);
+        emit_pawn_leaf(emit, lsb(m) - CW, lowbit(m), 0);
     for (u64 m = cap_e<S>(fp | (myp & (S ? f.pa : f.pd) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
-        emit_pawn(emit, lsb(m) - CE, lowbit(m), 0);
+        emit_pawn_leaf(emit, lsb(m) - CE, lowbit(m), 0);
     if (!f.checkers) {
         if (can_castle_k<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 62 : 6, MF_KCASTLE), PC_KING);
         if (can_castle_q<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 58 : 2, MF_QCASTLE), PC_KING);
@@ -849,20 +864,20 @@ __device__ __forceinline__ void make_move(Pos& b, u16 mv)
 // for the side to move next reads (the pieces, that side's castling rights
 // and the exact en-passant file, as make_move) and leaves the mover's own
 // castling rights and the side bit as they were.  `piece` is the moving piece
-// (PC_*), so nothing is looked up on the board to find it, plus PC_EP_FLAG on
-// a double push that gives the opponent an en-passant capture.
+// that lands on the target square (PC_*; the promoted piece for a
+// promotion), so nothing is looked up on the board or decoded from the flags,
+// plus PC_EP_FLAG on a double push that gives the opponent an en-passant
+// capture.
 template <int S>
 __device__ __forceinline__ void make_child(Pos& b, u16 mv, u32 piece)
 {
     const int from = mv & 63, to = (mv >> 6) & 63, fl = (mv >> 12) & 15;
     const u64 src = 1ull << from, dst = 1ull << to;
-    const bool promo = fl & 8;
-    const int pr = fl & 3;  // promotion piece: 0 N, 1 B, 2 R, 3 Q
     const u32 pc = piece & 7u;
-    const bool toN = promo ? pr == 0 : pc == PC_KNIGHT;
-    const bool toB = promo ? (pr & 1) != 0 : (pc == PC_BISHOP || pc == PC_QUEEN);
-    const bool toR = promo ? pr >= 2 : (pc == PC_ROOK || pc == PC_QUEEN);
-    const bool toP = !promo && pc == PC_PAWN;
+    const bool toN = pc == PC_KNIGHT;
+    const bool toB = pc == PC_BISHOP || pc == PC_QUEEN;
+    const bool toR = pc == PC_ROOK || pc == PC_QUEEN;
+    const bool toP = pc == PC_PAWN;
     const u64 clr = ~(src | dst);
     b.bq = (b.bq & clr) | (toB ? dst : 0ull);
     b.rq = (b.rq & clr) | (toR ? dst : 0ull);
@@ -883,7 +898,10 @@ __device__ __forceinline__ void make_child(Pos& b, u16 mv, u32 piece)
         if (!S) b.w = (b.w ^ rf) | rt;
     }
     set_ep(b, 0);
-    castle_update(b, dst, S);  // a capture on the other side's rook corner
+    // a move onto the other side's rook corner takes that side's right
+    // (updateCastleFlag, MGB.h:1310-1340): h8/a8 clear black's bits 2/3,
+    // h1/a1 clear white's bits 0/1
+    b.p &= S ? ~(((dst >> 7) & 1ull) | ((dst << 1) & 2ull)) : ~(((dst >> 61) & 4ull) | ((dst >> 53) & 8ull));
     if (piece & PC_EP_FLAG) set_ep(b, (from & 7) + 1);
 }
 
