@@ -101,6 +101,14 @@ struct QEmit {
     }
 };
 
+// QEmit when every move of the CTA's nodes fits the queue (one window)
+struct QEmitAll {
+    u32* q;
+    u32 pos, tag;
+    __device__ __forceinline__ void operator()(u16 m) { q[pos++] = tag | m; }
+    __device__ __forceinline__ void operator()(u16 m, u32 piece) { q[pos++] = tag | m | (piece << 25); }
+};
+
 struct ArrEmit {
     u16* out;
     u32 n;
@@ -308,7 +316,13 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
         // more children than the queue holds) make it again
         if (total) {
             const u32 hi = min((u32)QCAP, total);
-            if (c && off < hi) {
+            if (total <= (u32)QCAP) {  // one window: no position checks
+                if (c) {
+                    QEmitAll e{q, off, (u32)tid << 16};
+                    if constexpr (kFacts) gen_from_facts<S>(b, f, e);
+                    else gen_leaf<S>(b, e);
+                }
+            } else if (c && off < hi) {
                 QEmit e{q, off, 0u, hi, (u32)tid << 16};
                 if constexpr (kFacts) gen_from_facts<S>(b, f, e);
                 else gen_leaf<S>(b, e);
