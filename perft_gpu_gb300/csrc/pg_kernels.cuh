@@ -251,7 +251,12 @@ template <class SL, int T, int QCAP> struct BlockSmem {
 #endif
 template <int T> constexpr int min_blocks() { return (PG_LEAF_MIN_WARPS * 32 + T - 1) / T; }
 
-// the last plies of every node with remaining depth <= 2, inside one CTA
+// the last plies of every node with remaining depth <= 2, inside one CTA.
+// Each thread takes one node and counts its moves; the CTA scans the counts;
+// each thread writes its node's moves into the shared queue as (node, move,
+// landing piece, en-passant bit) entries; then every thread makes and counts
+// queued children, one at a time.  A CTA's children normally fit one queue
+// window; when they do not, the later windows generate again.
 template <int S, class SL, int T, int QCAP>
 __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
                                                             u32 max_rem)
