@@ -171,6 +171,16 @@ int pg_autotune(pg_tuning *out);
  * depend on what earlier calls stored).  No counterpart in the reference. */
 int pg_tt_clear(void);
 
+/* Snapshot of the transposition tables on disk, so a later process starts
+ * with the subtrees an earlier one counted (the reference's disk hash,
+ * launcher.h:699-790, keeps a chained table in a file instead; off there by
+ * default).  pg_tt_save writes the tables as they are (a header, then the
+ * tables: about the TT size in bytes); pg_tt_load reads a snapshot back,
+ * making tables of the snapshot's size, and rejects files that are not
+ * snapshots of this engine (format, Zobrist keys, depth range). */
+int pg_tt_save(const char *path);
+int pg_tt_load(const char *path);
+
 /* Divided perft at deep roots: perft_bb_cpu_launcher (launcher.h:1181-1389)
  * with its complete transposition table (launcher.h:598-680).  The positions
  * split_plies below each root move are made on the GPU and merged across all

@@ -159,6 +159,8 @@ _SIGNATURES = {
                        ctypes.POINTER(ctypes.c_double)],
     "pg_server_stop": [],
     "pg_tt_clear": [],
+    "pg_tt_save": [ctypes.c_char_p],
+    "pg_tt_load": [ctypes.c_char_p],
     "pg_autotune": [ctypes.POINTER(PgTuning)],
     "pg_perft_split": [_BP, ctypes.c_int, ctypes.c_int, _U16P, _U64P, _U32P, _OP],
     "pg_selftest": [ctypes.c_int],
@@ -344,6 +346,16 @@ def autotune() -> dict:
 def tt_clear():
     """Empty the transposition tables."""
     _check(load_library().pg_tt_clear())
+
+
+def tt_save(path: str):
+    """Write the transposition tables to a snapshot file."""
+    _check(load_library().pg_tt_save(os.fsencode(path)))
+
+
+def tt_load(path: str):
+    """Read a snapshot written by tt_save back into the tables."""
+    _check(load_library().pg_tt_load(os.fsencode(path)))
 
 
 def board_of(row) -> HexaBitBoardPosition:

@@ -1085,6 +1085,30 @@ int pg_tt_clear(void)
     return tt_clear();
 }
 
+int pg_tt_save(const char* path)
+{
+    if (!path) {
+        set_error("null argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    return tt_save(path);
+}
+
+int pg_tt_load(const char* path)
+{
+    if (!path) {
+        set_error("null argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    PG_TRY(check_ready());
+    return tt_load(path);
+}
+
 int pg_perft_batch_device(const pg_board* d_pos, const uint8_t* d_depths, uint32_t n, uint64_t* d_out,
                           const pg_opts* opts)
 {

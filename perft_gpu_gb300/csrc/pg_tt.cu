@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "pg_kernels.cuh"
@@ -259,11 +261,13 @@ static __global__ void k_tt_finish(LevelView lv, u32 n, LevelTT lt, TTSet tt, co
 
 static int small_grid(u64 n) { return (int)std::max<u64>(1, std::min<u64>((n + 255) / 256, 8192)); }
 
+constexpr u64 ZOBRIST_SEED = 0x5EED2B1D0C0FFEE5ull;
+
 int tt_upload_keys()
 {
     // 781 keys from splitmix64 with a fixed seed
     u64 keys[ZOBRIST_KEYS];
-    u64 s = 0x5EED2B1D0C0FFEE5ull;
+    u64 s = ZOBRIST_SEED;
     for (int i = 0; i < ZOBRIST_KEYS; i++) {
         u64 z = (s += 0x9E3779B97F4A7C15ull);
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -415,6 +419,126 @@ void tt_free()
     if (g_tt.root_of) cudaFree(g_tt.root_of);
     if (g_tt.counters) cudaFree(g_tt.counters);
     g_tt = TTState{};
+}
+
+// ---------------------------------------------------------------------------
+// snapshot of the tables on disk.  The reference keeps a chained table in a
+// file and probes it during the search (diskTTProbe, launcher.h:699-790, off
+// by default); here the HBM tables are written out whole and read back, so a
+// later process starts with the subtrees an earlier one counted.  The file is
+// a header (format, Zobrist seed, depth range, entries per table, the TT size
+// the tables were made for) followed by the tables as they lie in HBM.
+// ---------------------------------------------------------------------------
+
+struct TTFileHeader {
+    char magic[8];       // "PGTT" and the format version
+    u64 key_seed;        // entries are only valid under the same keys
+    u32 min_depth, max_depth;
+    u64 entries;         // per table (a power of two)
+    u64 budget_bytes;    // the TT size the tables were made for
+};
+static const char TT_MAGIC[8] = {'P', 'G', 'T', 'T', 0, 0, 0, 1};
+constexpr u64 TT_FILE_CHUNK = 64ull << 20;
+
+int tt_save(const char* path)
+{
+    Engine& E = engine();
+    if (!g_tt.pool) {
+        set_error("no transposition tables to save (run a perft with use_tt first)");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    TT_CUDA(cudaStreamSynchronize(E.stream));
+    const int ntab = TT_MAX_DEPTH - TT_MIN_DEPTH + 1;
+    TTFileHeader h{};
+    memcpy(h.magic, TT_MAGIC, sizeof(h.magic));
+    h.key_seed = ZOBRIST_SEED;
+    h.min_depth = TT_MIN_DEPTH;
+    h.max_depth = TT_MAX_DEPTH;
+    h.entries = g_tt.set.mask[TT_MIN_DEPTH] + 1;
+    h.budget_bytes = g_tt.pool_bytes;
+    const u64 total = h.entries * 16 * ntab;
+    FILE* f = fopen(path, "wb");
+    if (!f) {
+        set_error("cannot open %s for writing", path);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<unsigned char> buf((size_t)std::min(total, TT_FILE_CHUNK));
+    bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+    for (u64 off = 0; ok && off < total; off += TT_FILE_CHUNK) {
+        const u64 len = std::min(TT_FILE_CHUNK, total - off);
+        const cudaError_t e = cudaMemcpy(buf.data(), (unsigned char*)g_tt.pool + off, len, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            fclose(f);
+            set_error("reading the tables failed: %s", cudaGetErrorString(e));
+            return PG_ERR_CUDA;
+        }
+        ok = fwrite(buf.data(), 1, len, f) == len;
+    }
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) {
+        set_error("writing %s failed", path);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    return PG_OK;
+}
+
+int tt_load(const char* path)
+{
+    Engine& E = engine();
+    FILE* f = fopen(path, "rb");
+    if (!f) {
+        set_error("cannot open %s", path);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    TTFileHeader h{};
+    const int ntab = TT_MAX_DEPTH - TT_MIN_DEPTH + 1;
+    if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, TT_MAGIC, sizeof(h.magic)) != 0 ||
+        h.key_seed != ZOBRIST_SEED || h.min_depth != (u32)TT_MIN_DEPTH || h.max_depth != (u32)TT_MAX_DEPTH ||
+        h.entries < 1024 || (h.entries & (h.entries - 1))) {
+        fclose(f);
+        set_error("%s is not a transposition-table snapshot of this engine", path);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    if (!g_tt.keys_ready) {
+        const int r = tt_upload_keys();
+        if (r != PG_OK) {
+            fclose(f);
+            return r;
+        }
+    }
+    {
+        const int r = ensure_tables(h.budget_bytes);
+        if (r != PG_OK || g_tt.set.mask[TT_MIN_DEPTH] + 1 != h.entries) {
+            fclose(f);
+            if (r == PG_OK) set_error("%s: table layout does not match", path);
+            return r != PG_OK ? r : PG_ERR_INVALID_ARGUMENT;
+        }
+    }
+    const cudaError_t se = cudaStreamSynchronize(E.stream);
+    if (se != cudaSuccess) {
+        fclose(f);
+        set_error("cudaStreamSynchronize failed: %s", cudaGetErrorString(se));
+        return PG_ERR_CUDA;
+    }
+    const u64 total = h.entries * 16 * ntab;
+    std::vector<unsigned char> buf((size_t)std::min(total, TT_FILE_CHUNK));
+    for (u64 off = 0; off < total; off += TT_FILE_CHUNK) {
+        const u64 len = std::min(TT_FILE_CHUNK, total - off);
+        if (fread(buf.data(), 1, len, f) != len) {
+            fclose(f);
+            cudaMemset(g_tt.pool, 0, total);  // never leave half a snapshot
+            set_error("%s is shorter than its header says", path);
+            return PG_ERR_INVALID_ARGUMENT;
+        }
+        const cudaError_t e = cudaMemcpy((unsigned char*)g_tt.pool + off, buf.data(), len, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            fclose(f);
+            set_error("writing the tables failed: %s", cudaGetErrorString(e));
+            return PG_ERR_CUDA;
+        }
+    }
+    fclose(f);
+    return PG_OK;
 }
 
 int tt_clear()

@@ -59,3 +59,33 @@ def test_tt_config2_depth7(pg):
     pg.tt_clear()
     assert pg.perft(b, 7, use_tt=True) == g["perft7"]
     assert pg.perft(b, 6, use_tt=True) == g["perft6"]
+
+
+def test_tt_snapshot_save_load(pg, tmp_path):
+    """A snapshot written after a TT run and read back after clearing gives
+    TT hits on the first pass of the same run, with the same counts; files
+    that are not snapshots are refused."""
+    fens = {f["name"]: f for f in golden_json("fens.json")}
+    b = pg.board_from_fen(fens["position2"]["fen"])
+    want = fens["position2"]["perft"]["5"]
+    size = 64 << 20
+    pg.tt_clear()
+    assert pg.perft(b, 5, use_tt=True, tt_bytes=size) == want
+    snap = str(tmp_path / "tt.snap")
+    pg.tt_save(snap)
+    pg.tt_clear()
+    st0 = pg.PgStats()
+    assert pg.perft(b, 5, use_tt=True, tt_bytes=size, stats=st0) == want
+    assert st0.tt_hits == 0                     # cleared: a single pass finds nothing stored
+    pg.tt_clear()
+    pg.tt_load(snap)
+    st1 = pg.PgStats()
+    assert pg.perft(b, 5, use_tt=True, tt_bytes=size, stats=st1) == want
+    assert st1.tt_hits > 0                      # the snapshot's entries are found
+    bad = tmp_path / "bad.snap"
+    bad.write_bytes(b"not a snapshot" * 10)
+    with pytest.raises(pg.PerftError):
+        pg.tt_load(str(bad))
+    with pytest.raises(pg.PerftError):
+        pg.tt_load(str(tmp_path / "missing.snap"))
+    pg.tt_clear()
