@@ -3,6 +3,7 @@
 //
 //   perft_gpu [<fen> [<depth> [<numGPUs> [<launchDepth>]]]] [-divide] [-tt]
 //   perft_gpu -records <file> [<depth>] [-tt]
+//   ... [-ttload <snapshot>] [-ttsave <snapshot>]   (imply -tt) [-ttmib <MiB>]
 //
 // Like perft.cu it prints one "GPU Perft" line (launcher.h:1488-1498) per
 // depth from 3 to <depth>; depths of 9 and more go through the divided path
@@ -37,6 +38,8 @@ static std::string move_string(pg_move m)
              (to >> 3) + 1);
     return buf;
 }
+
+static uint64_t g_tt_bytes = 0;  // -ttmib: TT size (0 = from the engine's budget)
 
 static int fail(const char* what)
 {
@@ -77,6 +80,7 @@ static int records_mode(const char* file, int depth, bool tt)
     const double t0 = now_s();
     pg_opts o{};
     o.use_tt = tt ? 1 : 0;
+    o.tt_bytes = g_tt_bytes;
     const size_t B = 4096;
     for (size_t b0 = 0; b0 < lines.size(); b0 += B) {
         const size_t nb = std::min(B, lines.size() - b0);
@@ -108,22 +112,31 @@ int main(int argc, char** argv)
 {
     std::vector<const char*> pos;
     bool divide = false, tt = false, records = false;
+    const char* tt_load = nullptr;
+    const char* tt_save = nullptr;
     for (int i = 1; i < argc; i++) {
         if (!strcmp(argv[i], "-divide")) divide = true;
         else if (!strcmp(argv[i], "-tt")) tt = true;
         else if (!strcmp(argv[i], "-records")) records = true;
+        else if (!strcmp(argv[i], "-ttload") && i + 1 < argc) tt_load = argv[++i], tt = true;
+        else if (!strcmp(argv[i], "-ttsave") && i + 1 < argc) tt_save = argv[++i], tt = true;
+        else if (!strcmp(argv[i], "-ttmib") && i + 1 < argc) g_tt_bytes = (uint64_t)atoll(argv[++i]) << 20;
         else pos.push_back(argv[i]);
     }
     if (pg_init(nullptr) != PG_OK) return fail("pg_init");
+    if (tt_load && pg_tt_load(tt_load) != PG_OK) return fail("pg_tt_load");
+    auto finish = [&](int rc) {
+        if (rc == 0 && tt_save && pg_tt_save(tt_save) != PG_OK) rc = fail("pg_tt_save");
+        pg_shutdown();
+        return rc;
+    };
     if (records) {
         if (pos.empty()) {
             printf("usage: perft_gpu -records <inFile> [depth] [-tt]\n");
             return 1;
         }
         const int depth = pos.size() > 1 ? atoi(pos[1]) : 7;
-        const int rc = records_mode(pos[0], depth, tt);
-        pg_shutdown();
-        return rc;
+        return finish(records_mode(pos[0], depth, tt));
     }
     const char* start = "rnbqkbnr/pppppppp/8/8/8/8/PPPPPPPP/RNBQKBNR w KQkq - 0 1";
     const char* fen = (!pos.empty() && strlen(pos[0]) > 5) ? pos[0] : start;
@@ -134,6 +147,7 @@ int main(int argc, char** argv)
     if (pg_board_from_fen(fen, &b) != PG_OK) return fail("FEN");
     pg_opts o{};
     o.use_tt = tt ? 1 : 0;
+    o.tt_bytes = g_tt_bytes;
     const int minDepth = maxDepth < 3 ? maxDepth : 3;
     for (int depth = minDepth; depth <= maxDepth; depth++) {
         const double t0 = now_s();
@@ -159,6 +173,5 @@ int main(int argc, char** argv)
         }
         fflush(stdout);
     }
-    pg_shutdown();
-    return 0;
+    return finish(0);
 }

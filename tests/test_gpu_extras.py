@@ -98,3 +98,21 @@ def test_python_cli_tt_options(tmp_path):
     assert "GPU Perft 4: %d," % fens["position3"]["perft"]["4"] in out.stdout
     assert "GPU Perft 5: %d," % fens["position3"]["perft"]["5"] in out.stdout
     assert "tt_probes=" in out.stdout and "tt_stores=" in out.stdout
+
+
+def test_cli_tt_snapshot_between_runs(tmp_path):
+    """perft_gpu -ttsave writes the tables at exit; a second run with -ttload
+    starts from them and prints the same counts."""
+    fens = {f["name"]: f for f in golden_json("fens.json")}
+    snap = str(tmp_path / "tt.snap")
+    fen = fens["position4"]["fen"]
+    r1 = subprocess.run([CLI, fen, "5", "-ttmib", "64", "-ttsave", snap], capture_output=True, text=True,
+                        timeout=300)
+    assert r1.returncode == 0, r1.stderr
+    assert 0 < os.path.getsize(snap) <= (64 << 20) + 4096
+    r2 = subprocess.run([CLI, fen, "5", "-ttmib", "64", "-ttload", snap], capture_output=True, text=True,
+                        timeout=300)
+    assert r2.returncode == 0, r2.stderr
+    for d in (3, 4, 5):
+        line = "GPU Perft %d: %d," % (d, fens["position4"]["perft"][str(d)])
+        assert line in r1.stdout and line in r2.stdout
