@@ -400,6 +400,8 @@ int pg_server_start(const pg_server_config* cfg)
     cudaError_t e = cudaSetDevice(E.device);
     if (e == cudaSuccess) e = cudaMalloc(&S->acc, S->max_inflight * sizeof(u64));
     if (e == cudaSuccess) e = cudaMemset(S->acc, 0, S->max_inflight * sizeof(u64));
+    // the engine's kernels run on a non-blocking stream: finish the clear here
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e == cudaSuccess) e = cudaMalloc(&S->pool, S->pool_cap * sizeof(Pos));
     if (e == cudaSuccess) e = cudaMalloc(&S->wave_pos, MAX_WAVE_TASKS * sizeof(Pos));
     if (e == cudaSuccess) e = cudaMalloc(&S->wave_dep, MAX_WAVE_TASKS);

@@ -466,7 +466,10 @@ int tt_save(const char* path)
     bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
     for (u64 off = 0; ok && off < total; off += TT_FILE_CHUNK) {
         const u64 len = std::min(TT_FILE_CHUNK, total - off);
-        const cudaError_t e = cudaMemcpy(buf.data(), (unsigned char*)g_tt.pool + off, len, cudaMemcpyDeviceToHost);
+        // on the engine's stream, completed before the buffer is written out
+        cudaError_t e = cudaMemcpyAsync(buf.data(), (unsigned char*)g_tt.pool + off, len, cudaMemcpyDeviceToHost,
+                                        E.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(E.stream);
         if (e != cudaSuccess) {
             fclose(f);
             set_error("reading the tables failed: %s", cudaGetErrorString(e));
@@ -526,11 +529,16 @@ int tt_load(const char* path)
         const u64 len = std::min(TT_FILE_CHUNK, total - off);
         if (fread(buf.data(), 1, len, f) != len) {
             fclose(f);
-            cudaMemset(g_tt.pool, 0, total);  // never leave half a snapshot
+            // never leave half a snapshot
+            if (cudaMemsetAsync(g_tt.pool, 0, total, E.stream) == cudaSuccess) cudaStreamSynchronize(E.stream);
             set_error("%s is shorter than its header says", path);
             return PG_ERR_INVALID_ARGUMENT;
         }
-        const cudaError_t e = cudaMemcpy((unsigned char*)g_tt.pool + off, buf.data(), len, cudaMemcpyHostToDevice);
+        // on the engine's stream (the engine's kernels run on a non-blocking
+        // stream), completed before the buffer is reused
+        cudaError_t e = cudaMemcpyAsync((unsigned char*)g_tt.pool + off, buf.data(), len, cudaMemcpyHostToDevice,
+                                        E.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(E.stream);
         if (e != cudaSuccess) {
             fclose(f);
             set_error("writing the tables failed: %s", cudaGetErrorString(e));
