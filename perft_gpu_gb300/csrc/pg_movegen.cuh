@@ -54,7 +54,10 @@ static inline cudaError_t upload_static_tables(const HostTables& t)
     if ((e = cudaMemcpyToSymbol(g_king, t.king, sizeof(t.king)))) return e;
     if ((e = cudaMemcpyToSymbol(g_diag, t.diag, sizeof(t.diag)))) return e;
     if ((e = cudaMemcpyToSymbol(g_pawn_checks, t.pawn_checks, sizeof(t.pawn_checks)))) return e;
-    return cudaMemcpyToSymbol(g_knight, t.knight, sizeof(t.knight));
+    if ((e = cudaMemcpyToSymbol(g_knight, t.knight, sizeof(t.knight)))) return e;
+    // uploads from pageable memory may still be in flight when these calls
+    // return, and the kernels run on non-blocking streams: finish them here
+    return cudaStreamSynchronize(0);
 }
 
 // Kogge-Stone: pure shift/and/or, no memory traffic.
