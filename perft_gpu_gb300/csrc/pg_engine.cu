@@ -818,11 +818,45 @@ int pg_get_stream(void** stream)
     return PG_OK;
 }
 
-int pg_init(const pg_config* cfg)
+// every resource the engine holds; handles that were never made are null
+static void release_engine(Engine& E)
 {
-    Engine& E = engine();
-    std::lock_guard<std::mutex> lk(E.mu);
-    if (E.ready) return PG_OK;
+    if (E.stream) cudaStreamSynchronize(E.stream);
+    for (auto& lb : E.lv) {
+        if (lb.block) cudaFree(lb.block);
+        lb = LevelBuf{};
+    }
+    tt_free();
+    if (E.scan_status) cudaFree(E.scan_status);
+    if (E.stage) cudaFree(E.stage);
+    if (E.tickets) cudaFree(E.tickets);
+    if (E.err) cudaFree(E.err);
+    if (E.plan_dev) cudaFree(E.plan_dev);
+    if (E.plan_host) cudaFreeHost(E.plan_host);
+    if (E.host_scratch) cudaFreeHost(E.host_scratch);
+    if (E.aux) cudaFree(E.aux);
+    if (E.graph.exec) cudaGraphExecDestroy(E.graph.exec);
+    E.graph = GraphCache{};
+    for (cudaEvent_t* ev : {&E.ev0, &E.ev1, &E.lev0, &E.lev1})
+        if (*ev) cudaEventDestroy(*ev), *ev = nullptr;
+    if (E.stream) cudaStreamDestroy(E.stream);
+    E.stream = nullptr;
+    E.tickets = nullptr;
+    E.err = nullptr;
+    E.plan_dev = nullptr;
+    E.plan_host = nullptr;
+    E.host_scratch = nullptr;
+    E.aux = nullptr;
+    E.scan_status = nullptr;
+    E.scan_status_cap = 0;
+    E.stage = nullptr;
+    E.stage_cap = 0;
+    E.level_bytes_total = 0;
+    E.ready = false;
+}
+
+static int init_locked(Engine& E, const pg_config* cfg)
+{
     E.device = cfg ? cfg->device : 0;
     E.verbose = cfg ? cfg->verbose : 0;
     E.default_slider = cfg ? cfg->slider : PG_SLIDER_AUTO;
@@ -868,38 +902,22 @@ int pg_init(const pg_config* cfg)
     return PG_OK;
 }
 
+int pg_init(const pg_config* cfg)
+{
+    Engine& E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    if (E.ready) return PG_OK;
+    const int rc = init_locked(E, cfg);
+    if (rc != PG_OK) release_engine(E);  // a later pg_init starts clean
+    return rc;
+}
+
 int pg_shutdown(void)
 {
     Engine& E = engine();
     std::lock_guard<std::mutex> lk(E.mu);
     if (!E.ready) return PG_OK;
-    cudaStreamSynchronize(E.stream);
-    for (auto& lb : E.lv) {
-        if (lb.block) cudaFree(lb.block);
-        lb = LevelBuf{};
-    }
-    tt_free();
-    if (E.scan_status) cudaFree(E.scan_status);
-    if (E.stage) cudaFree(E.stage);
-    cudaFree(E.tickets);
-    cudaFree(E.err);
-    cudaFree(E.plan_dev);
-    cudaFreeHost(E.plan_host);
-    cudaFreeHost(E.host_scratch);
-    cudaFree(E.aux);
-    if (E.graph.exec) cudaGraphExecDestroy(E.graph.exec);
-    E.graph = GraphCache{};
-    cudaEventDestroy(E.ev0);
-    cudaEventDestroy(E.ev1);
-    cudaEventDestroy(E.lev0);
-    cudaEventDestroy(E.lev1);
-    cudaStreamDestroy(E.stream);
-    E.scan_status = nullptr;
-    E.scan_status_cap = 0;
-    E.stage = nullptr;
-    E.stage_cap = 0;
-    E.level_bytes_total = 0;
-    E.ready = false;
+    release_engine(E);
     return PG_OK;
 }
 
