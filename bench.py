@@ -150,6 +150,19 @@ def max_over_ranks(dist, x: float) -> float:
     return float(t.item())
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), recorded beside every CPU number."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def cpu_leaves_per_s(boards, depths, threads, prefer_reference=True):
     """The reference's CPU perft over a sample of the workload: oracle/_ref when
     it was built here (the reference compiled from its sources), else the
@@ -203,6 +216,7 @@ def run_reference(args):
                    "sample": "each step: positions i = step (mod %d)" % stride},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "leaf nodes/s", "cores": threads, "kind": kind,
+                         "cpu_model": cpu_model(),
                          "sample": "1/%d of the 4096 positions per step (%d steps)" % (stride, args.steps)},
         "e2e": {"value": value, "unit": "leaf nodes/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -336,7 +350,8 @@ def workloads_leg(pg, threads):
     out["64_positions_depth5"] = {
         "leaves": c1["total"], "gpu_leaves_per_s": c1["total"] / s1, "gpu_wall_s": s1,
         "gpu_device_ms": st.device_ms,
-        "cpu": {"kind": cpu_all[2], "threads": threads, "leaves_per_s": c1["total"] / cpu_all[1],
+        "cpu": {"kind": cpu_all[2], "threads": threads, "cpu_model": cpu_model(),
+                "leaves_per_s": c1["total"] / cpu_all[1],
                 "one_thread_leaves_per_s": c1["total"] / cpu_one[1]}}
 
     # one deep position (seed 2, 30 plies, >= 35 moves) at depth 7
@@ -565,6 +580,7 @@ def run_ours(args):
             if g is not None:
                 assert np.array_equal(cout, g[0][idx])
             cpu = {"value": int(cout.sum()) / csecs, "unit": "leaf nodes/s", "cores": threads,
+                   "cpu_model": cpu_model(),
                    "kind": kind,
                    "sample": "every %dth of the 4096 positions (%d positions, %d leaves)"
                              % (args.cpu_stride, len(idx), int(cout.sum()))}
