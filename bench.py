@@ -346,12 +346,16 @@ def workloads_leg(pg, threads):
     assert int(r1.sum()) == c1["total"]
     cpu_all = cpu_leaves_per_s(b1, d1, threads)
     cpu_one = cpu_leaves_per_s(b1, d1, 1)
+    import oracle as O
+    ks_out, ks_secs = O.Oracle(0).perft_batch(b1, d1, threads)  # the C restatement with Kogge-Stone sliders
     assert int(cpu_all[0].sum()) == c1["total"] and int(cpu_one[0].sum()) == c1["total"]
+    assert int(ks_out.sum()) == c1["total"]
     out["64_positions_depth5"] = {
         "leaves": c1["total"], "gpu_leaves_per_s": c1["total"] / s1, "gpu_wall_s": s1,
         "gpu_device_ms": st.device_ms,
         "cpu": {"kind": cpu_all[2], "threads": threads, "cpu_model": cpu_model(),
                 "leaves_per_s": c1["total"] / cpu_all[1],
+                "kogge_stone_port_leaves_per_s": c1["total"] / ks_secs,
                 "one_thread_leaves_per_s": c1["total"] / cpu_one[1]}}
 
     # one deep position (seed 2, 30 plies, >= 35 moves) at depth 7
