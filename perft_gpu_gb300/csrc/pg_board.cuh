@@ -158,6 +158,33 @@ __device__ __forceinline__ void vertical_fills(u64 empty, u64 g, u64& up_att, u6
     down_att = c >> 8;
 }
 
+// the same two chains kept for several generator sets
+struct VPro {
+    u64 e, p2, p4, q2, q4;
+    __device__ __forceinline__ explicit VPro(u64 empty)
+    {
+        e = empty;
+        p2 = empty & (empty << 8);
+        p4 = p2 & (p2 << 16);
+        q2 = p2 >> 8;
+        q4 = p4 >> 24;
+    }
+    __device__ __forceinline__ u64 up(u64 g) const
+    {
+        g |= e & (g << 8);
+        g |= p2 & (g << 16);
+        g |= p4 & (g << 32);
+        return g << 8;
+    }
+    __device__ __forceinline__ u64 down(u64 g) const
+    {
+        g |= e & (g >> 8);
+        g |= q2 & (g >> 16);
+        g |= q4 & (g >> 32);
+        return g >> 8;
+    }
+};
+
 __device__ __forceinline__ u64 ks_rook(u64 g, u64 empty)
 {
     return ray<8, true>(g, empty) | ray<8, false>(g, empty) | ray<1, true>(g, empty) | ray<1, false>(g, empty);

@@ -467,6 +467,142 @@ __device__ __forceinline__ u32 count_moves_ks(const Pos& b)
     return count_from_facts<S, OWN_BY_LOOKUP>(b, ks_facts<S>(b));
 }
 
+// Rank attacks by subtraction: with file H marked occupied (so that no borrow
+// leaves a rank), `o - 2g` borrows from each slider's next square up to its
+// first blocker, and `o ^ (o - 2g)` is every slider's eastward ray, blocker
+// included.  Rays of different sliders are disjoint, so the borrows never
+// meet.  Westward rays are the same on the bit-reversed board (file A <-> H).
+struct RankPro {
+    u64 oe, ow;
+    __device__ __forceinline__ explicit RankPro(u64 occ)
+    {
+        oe = occ | FILE_H;
+        ow = __brevll(occ | FILE_A);
+    }
+    __device__ __forceinline__ u64 east(u64 g) const { return oe ^ (oe - ((g << 1) & NOT_A)); }
+    __device__ __forceinline__ u64 west(u64 g) const
+    {
+        return __brevll(ow ^ (ow - ((__brevll(g) << 1) & NOT_A)));
+    }
+};
+
+// The same count with one propagator chain per direction, built from the
+// real empty squares and shared by the enemy's sliders (attacks, pins) and
+// the side to move's sliders (moves).  Three differences from ks_facts +
+// count_from_facts make that possible:
+//  * the king is opaque to the enemy fills, so the square behind the king on
+//    a slider-checking line is added to the enemy attacks by hand (the
+//    king's neighbour on the same king ray, on the far side from the checker);
+//    outside check no enemy fill reaches the king and nothing differs;
+//  * own sliders are filled as if none were pinned: rays of different
+//    sliders along one direction are disjoint, so the filled popcounts are the
+//    sum of every slider's own moves, and a pinned slider's moves off its pin
+//    line (all of them in check) are taken back with one lookup per pinned
+//    slider (rare);
+//  * the checkers and the target mask come first (from the king's rays), so
+//    each direction's own fill is counted as soon as it is made.
+template <int S>
+__device__ __forceinline__ u32 count_moves_ks1(const Pos& b)
+{
+    const u64 pawns = b.p & INNER;
+    const u64 occ = b.k | pawns | b.n | b.bq | b.rq;
+    const u64 black = occ & ~b.w;
+    const u64 mine = S ? black : b.w, theirs = S ? b.w : black;
+    const u64 king = b.k & mine;
+    const u64 empty = ~occ;
+    const u64 trq = b.rq & theirs, tbq = b.bq & theirs;
+    const u64 my_rq = b.rq & mine, my_bq = b.bq & mine;
+    const u64 tp = pawns & theirs, tn = b.n & theirs;
+
+    // the king's rays, split per line, and the checkers
+    const int ksq = sq_of(king);
+    const u64 kr = SlFancy::rook(ksq, occ), kb = SlFancy::bishop(ksq, occ);
+    const u64 kf = kr & file_of(ksq), kd = kb & __ldg(&g_diag[ksq]);
+    const u64 kh = kr ^ kf, ka = kb ^ kd;
+    const u64 cr = kr & trq, cb = kb & tbq;
+    const u64 csl = cr | cb;
+    const u64 checkers = csl | (__ldg(&g_knight[ksq]) & tn) | (__ldg(&g_pawn_checks[S][ksq]) & tp);
+    u64 cray = 0, behind = 0;
+    if (__any_sync(__activemask(), csl != 0)) {
+        const int csq = lsb(csl) & 63;
+        cray = SlFancy::look(cr ? g_magic_rook : g_magic_bishop, csq, occ) & (cr ? kr : kb);
+        for (u64 s = csl; s; s &= s - 1) {
+            const u64 c = s & (0ull - s);
+            const u64 kray = (c & kf) ? kf : (c & kh) ? kh : (c & kd) ? kd : ka;
+            behind |= kray & (c > king ? king - 1ull : ~(king | (king - 1ull)));
+        }
+    }
+    const bool in_check = checkers != 0;
+    const u64 chk_all = in_check ? ~0ull : 0ull;
+    const u64 safe = (csl ? cray : 0ull) | checkers;
+    const u64 tgt = several(checkers) ? 0ull : (in_check ? safe : ~mine);
+
+    u32 n = 0;
+    u64 threat, pf, pr, pd, pa;
+    {
+        const VPro v(empty);
+        const u64 a_v = v.up(trq) | v.down(trq);
+        pf = kf & a_v & mine;
+        threat = a_v;
+        n += popc(v.up(my_rq) & tgt) + popc(v.down(my_rq) & tgt);
+    }
+    {
+        const RankPro h(occ);
+        const u64 a_h = h.east(trq) | h.west(trq);
+        pr = kh & a_h & mine;
+        threat |= a_h;
+        n += popc(h.east(my_rq) & tgt) + popc(h.west(my_rq) & tgt);
+    }
+    {
+        const Pro<9, true> l(empty);
+        const Pro<9, false> r(empty);
+        const u64 a_d = l.attacks(tbq) | r.attacks(tbq);
+        pd = kd & a_d & mine;
+        threat |= a_d;
+        n += popc(l.attacks(my_bq) & tgt) + popc(r.attacks(my_bq) & tgt);
+    }
+    {
+        const Pro<7, true> l(empty);
+        const Pro<7, false> r(empty);
+        const u64 a_a = l.attacks(tbq) | r.attacks(tbq);
+        pa = ka & a_a & mine;
+        threat |= a_a;
+        n += popc(l.attacks(my_bq) & tgt) + popc(r.attacks(my_bq) & tgt);
+    }
+    const u64 pinned = pf | pr | pd | pa;
+    threat |= pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[sq_of(b.k & theirs)]);
+    n += popc(__ldg(&g_king[ksq]) & ~(threat | behind | mine));
+
+    // pinned sliders: take back the moves off the pin line (all in check)
+    for (u64 s = pinned & (my_rq | my_bq); s; s &= s - 1) {
+        const int sq = lsb(s);
+        const u64 bit = 1ull << sq;
+        u64 att = (my_rq & bit) ? SlFancy::rook(sq, occ) : 0ull;
+        if (my_bq & bit) att |= SlFancy::bishop(sq, occ);
+        const u64 line = (pf & bit) ? file_of(ksq) : (pr & bit) ? rank_of(ksq)
+                       : (pd & bit) ? __ldg(&g_diag[ksq]) : anti_of(ksq);
+        n -= popc(att & tgt & ~(line & ~chk_all));
+    }
+
+    for (u64 s = b.n & mine & ~pinned; s; s &= s - 1) n += popc(__ldg(&g_knight[lsb(s)]) & tgt);
+
+    // pawns, castling and en passant as in count_from_facts
+    const u64 myp = pawns & mine;
+    const u64 fp = myp & ~pinned;
+    const u64 pin_ok = ~chk_all;
+    const u64 d1 = push1<S>(fp | (myp & pf & pin_ok)) & empty;
+    const u64 s1 = d1 & tgt;
+    n += popc(s1) + 3 * popc(s1 & BACK_RANKS);
+    n += popc(push1<S>(d1 & double_rank<S>() & ~safe) & empty & tgt);
+    const u64 cw = cap_w<S>(fp | (myp & (S ? pd : pa) & pin_ok)) & theirs & tgt;
+    const u64 ce = cap_e<S>(fp | (myp & (S ? pa : pd) & pin_ok)) & theirs & tgt;
+    n += popc(cw) + popc(ce) + 3 * (popc(cw & BACK_RANKS) + popc(ce & BACK_RANKS));
+
+    if (!in_check) n += can_castle_k<S>(b, occ, threat) + can_castle_q<S>(b, occ, threat);
+    if (b.p & 0xF0ull) n += count_ep_ks<S>(b, pinned, checkers);
+    return n;
+}
+
 // countMoves / countMovesOutOfCheck (MGB.h:3008-3295, 2825-3002) for the
 // table policies, in the same mask form as count_moves_ks: one lookup per
 // slider for the enemy attacks and for the own moves (the 64-bit multiply
@@ -555,7 +691,7 @@ __device__ __forceinline__ u32 count_moves_mg(const Pos& b)
 template <int S, class SL>
 __device__ __forceinline__ u32 count_moves(const Pos& b)
 {
-    if constexpr (SL::kId == 0) return count_moves_ks<S, false>(b);
+    if constexpr (SL::kId == 0) return count_moves_ks1<S>(b);
     else if constexpr (SL::kId == 3) return count_moves_ks<S, true>(b);
     else return count_moves_mg<S, SL>(b);
 }
