@@ -185,6 +185,37 @@ struct VPro {
     }
 };
 
+// both directions of one diagonal line kind (SH = 9 or 7) from one chain.
+// The chain holds the squares a ray passes THROUGH: empty and on neither edge
+// file (a ray's inner squares never lie on the edge it moves away from, and
+// it cannot pass the edge it moves toward), so it is the same for both
+// directions and the backward chain is the forward one shifted back.
+template <int SH> struct DPro {
+    u64 p1, p2, p4, q2, q4;
+    __device__ __forceinline__ explicit DPro(u64 pass)
+    {
+        p1 = pass;
+        p2 = pass & (pass << SH);
+        p4 = p2 & (p2 << (2 * SH));
+        q2 = p2 >> SH;
+        q4 = p4 >> (3 * SH);
+    }
+    __device__ __forceinline__ u64 up(u64 g) const
+    {
+        g |= p1 & (g << SH);
+        g |= p2 & (g << (2 * SH));
+        g |= p4 & (g << (4 * SH));
+        return (g << SH) & DirMask<SH, true>::keep;
+    }
+    __device__ __forceinline__ u64 down(u64 g) const
+    {
+        g |= p1 & (g >> SH);
+        g |= q2 & (g >> (2 * SH));
+        g |= q4 & (g >> (4 * SH));
+        return (g >> SH) & DirMask<SH, false>::keep;
+    }
+};
+
 __device__ __forceinline__ u64 ks_rook(u64 g, u64 empty)
 {
     return ray<8, true>(g, empty) | ray<8, false>(g, empty) | ray<1, true>(g, empty) | ray<1, false>(g, empty);

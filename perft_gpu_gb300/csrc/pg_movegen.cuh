@@ -553,21 +553,20 @@ __device__ __forceinline__ u32 count_moves_ks1(const Pos& b)
         threat |= a_h;
         n += popc(h.east(my_rq) & tgt) + popc(h.west(my_rq) & tgt);
     }
+    const u64 pass = empty & NOT_A & NOT_H;
     {
-        const Pro<9, true> l(empty);
-        const Pro<9, false> r(empty);
-        const u64 a_d = l.attacks(tbq) | r.attacks(tbq);
+        const DPro<9> d(pass);
+        const u64 a_d = d.up(tbq) | d.down(tbq);
         pd = kd & a_d & mine;
         threat |= a_d;
-        n += popc(l.attacks(my_bq) & tgt) + popc(r.attacks(my_bq) & tgt);
+        n += popc(d.up(my_bq) & tgt) + popc(d.down(my_bq) & tgt);
     }
     {
-        const Pro<7, true> l(empty);
-        const Pro<7, false> r(empty);
-        const u64 a_a = l.attacks(tbq) | r.attacks(tbq);
+        const DPro<7> d(pass);
+        const u64 a_a = d.up(tbq) | d.down(tbq);
         pa = ka & a_a & mine;
         threat |= a_a;
-        n += popc(l.attacks(my_bq) & tgt) + popc(r.attacks(my_bq) & tgt);
+        n += popc(d.up(my_bq) & tgt) + popc(d.down(my_bq) & tgt);
     }
     const u64 pinned = pf | pr | pd | pa;
     threat |= pawn_attacks<1 - S>(tp) | knight_set(tn) | __ldg(&g_king[sq_of(b.k & theirs)]);
