@@ -214,10 +214,12 @@ int pg_random_playouts(uint64_t seed, uint32_t n, int min_plies, int max_plies, 
 
 /* ---- serving: continuous batching of perft requests ---- */
 typedef struct pg_server_config {
-    uint64_t hbm_budget_bytes;   /* admission budget for in-flight frontiers; 0 = engine budget */
+    uint64_t hbm_budget_bytes;   /* admission budget for in-flight frontiers; 0 = 2 GiB */
     uint32_t max_inflight;       /* request slots; 0 = 4096 */
     int slider;
-    uint32_t max_wave_nodes;     /* frontier nodes the scheduler advances per wave; 0 = auto */
+    uint32_t max_wave_nodes;     /* fixed wave size in frontier nodes (positions 5 plies above the
+                                    leaves); 0 = waves sized in time, about 4 ms of device work
+                                    each from the measured rate and leaves per task */
     int use_tt;                  /* count the waves through the transposition tables, which persist
                                     across requests (launcher.h:699-790 keeps its table across runs) */
     uint64_t tt_bytes;           /* TT size when use_tt; 0 = from the engine budget (as pg_opts) */

@@ -209,6 +209,39 @@ static Variant leaf_variant(const Variant& v, int L)
     return w;
 }
 
+// adds the leaf launches timed since the last call to the stats; every
+// recorded event must be complete (the caller synchronised the stream)
+static void collect_leaf_timers()
+{
+    Engine& E = engine();
+    for (size_t i = 0; i + 1 < E.leaf_ev_used; i += 2) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, E.leaf_ev[i], E.leaf_ev[i + 1]) == cudaSuccess)
+            E.st.leaf_kernel_ms += ms;
+        else
+            (void)cudaGetLastError();  // a pair left unrecorded by a failed call: no stale error
+    }
+    E.leaf_ev_used = 0;
+}
+
+// an event pair for the next leaf launch (created on first use, kept)
+static int leaf_timer_pair(cudaEvent_t*& pair)
+{
+    Engine& E = engine();
+    if (E.leaf_ev_used >= 512) {  // bound the pool: wait for the recorded ones
+        PG_CUDA(cudaEventSynchronize(E.leaf_ev[E.leaf_ev_used - 1]));
+        collect_leaf_timers();
+    }
+    while (E.leaf_ev.size() < E.leaf_ev_used + 2) {
+        cudaEvent_t ev;
+        PG_CUDA(cudaEventCreate(&ev));
+        E.leaf_ev.push_back(ev);
+    }
+    pair = &E.leaf_ev[E.leaf_ev_used];
+    E.leaf_ev_used += 2;
+    return PG_OK;
+}
+
 static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int minrem, int maxrem, u64* acc)
 {
     Engine& E = engine();
@@ -218,15 +251,13 @@ static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int mi
     const int lp = v.leaf_plies;
     const bool capturing = E.plan_mode == PLAN_REPLAY;
     if (minrem <= lp) {
-        if (!capturing) cudaEventRecord(E.lev0, E.stream);
-        PG_TRY(launch_leaf(leaf_variant(v, L), side, lb.v, start, n, acc));
+        cudaEvent_t* ev = nullptr;
         if (!capturing) {
-            cudaEventRecord(E.lev1, E.stream);
-            float ms = 0;
-            PG_CUDA(cudaEventSynchronize(E.lev1));
-            cudaEventElapsedTime(&ms, E.lev0, E.lev1);
-            E.st.leaf_kernel_ms += ms;
+            PG_TRY(leaf_timer_pair(ev));
+            cudaEventRecord(ev[0], E.stream);
         }
+        PG_TRY(launch_leaf(leaf_variant(v, L), side, lb.v, start, n, acc));
+        if (!capturing) cudaEventRecord(ev[1], E.stream);
     }
     if (maxrem <= lp) return PG_OK;
     PG_TRY(launch_count(v, side, lb.v, start, n, lb.cnt));
@@ -247,10 +278,12 @@ static int run_range(const Variant& v, int L, u32 start, u32 n, int side, int mi
         k_plan<<<1, 32, 0, E.stream>>>(lb.offs, n, cap_next, E.plan_dev, E.err);
         PG_CUDA(cudaGetLastError());
         E.st.launches++;
+        u32* perr = (u32*)(E.host_scratch + 192);  // pinned
         PG_CUDA(cudaMemcpyAsync(E.plan_host, E.plan_dev, sizeof(PlanOut), cudaMemcpyDeviceToHost, E.stream));
+        PG_CUDA(cudaMemcpyAsync(perr, E.err, sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
         PG_CUDA(cudaStreamSynchronize(E.stream));
-        u32 errv = 0;
-        PG_CUDA(cudaMemcpy(&errv, E.err, sizeof(u32), cudaMemcpyDeviceToHost));
+        collect_leaf_timers();
+        const u32 errv = *perr;
         if (errv) {
             set_error("device error flags 0x%x while planning level %d", errv, L);
             return PG_ERR_DEVICE_TIMEOUT;
@@ -431,6 +464,7 @@ static int begin_call(const pg_opts* o)
 {
     Engine& E = engine();
     E.st = pg_stats{};
+    E.leaf_ev_used = 0;
     E.ticket_next = 0;
     PG_CUDA(cudaMemsetAsync(E.tickets, 0, MAX_TICKETS * sizeof(u32), E.stream));
     PG_CUDA(cudaMemsetAsync(E.err, 0, sizeof(u32), E.stream));
@@ -460,6 +494,7 @@ int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_gro
 {
     Engine& E = engine();
     const bool capturing = E.plan_mode == PLAN_REPLAY;
+    E.leaf_ev_used = 0;
     PG_TRY(ensure_level(0, n));
     if (zero_acc) PG_CUDA(cudaMemsetAsync(acc, 0, (u64)n * sizeof(u64), E.stream));
     u32* ctr = (u32*)(E.host_scratch + 64);  // pinned, 4 words
@@ -496,6 +531,7 @@ int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_gro
         float ms = 0;
         cudaEventElapsedTime(&ms, E.ev0, E.ev1);
         E.st.device_ms = ms;
+        collect_leaf_timers();
     }
     return PG_OK;
 }
@@ -837,8 +873,11 @@ static void release_engine(Engine& E)
     if (E.aux) cudaFree(E.aux);
     if (E.graph.exec) cudaGraphExecDestroy(E.graph.exec);
     E.graph = GraphCache{};
-    for (cudaEvent_t* ev : {&E.ev0, &E.ev1, &E.lev0, &E.lev1})
+    for (cudaEvent_t* ev : {&E.ev0, &E.ev1})
         if (*ev) cudaEventDestroy(*ev), *ev = nullptr;
+    for (cudaEvent_t ev : E.leaf_ev) cudaEventDestroy(ev);
+    E.leaf_ev.clear();
+    E.leaf_ev_used = 0;
     if (E.stream) cudaStreamDestroy(E.stream);
     E.stream = nullptr;
     E.tickets = nullptr;
@@ -880,8 +919,6 @@ static int init_locked(Engine& E, const pg_config* cfg)
     PG_CUDA(cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking));
     PG_CUDA(cudaEventCreate(&E.ev0));
     PG_CUDA(cudaEventCreate(&E.ev1));
-    PG_CUDA(cudaEventCreate(&E.lev0));
-    PG_CUDA(cudaEventCreate(&E.lev1));
     const HostTables* tabs = host_tables();
     if (!tabs) {
         set_error("magic table construction failed");

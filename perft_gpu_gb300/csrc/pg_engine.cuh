@@ -76,7 +76,11 @@ struct Engine {
     int default_slider = PG_SLIDER_AUTO;
     u64 budget = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, lev0 = nullptr, lev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // start/end event pairs around leaf launches, read after the next host
+    // synchronisation instead of waiting on each launch
+    std::vector<cudaEvent_t> leaf_ev;
+    size_t leaf_ev_used = 0;
     LevelBuf lv[MAX_LEVELS];
     u64 level_bytes_total = 0;
     // scratch

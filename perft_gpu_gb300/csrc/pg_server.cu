@@ -6,12 +6,17 @@
 // are counted, so a request's frontier lives on the device for its whole
 // life.  Admission is gated by free request slots and by free space in the
 // pool (the server's HBM budget).  The scheduler thread runs waves: each wave
-// takes a fair share of the remaining tasks of every active request (a
-// request admitted a moment ago gets tasks in the very next wave, whatever
-// deep requests are running), runs them as one batched engine call that adds
-// each task's count into its request's device counter, and completes the
-// requests whose last task was in the wave.  New requests join at every wave
-// boundary, so their work overlaps on the device with the running ones.
+// takes one task of every active request (a request admitted a moment ago
+// gets work in the very next wave, whatever deep requests are running), then
+// fills its budget by least remaining work first, runs the tasks as one
+// batched engine call that adds each task's count into its request's device
+// counter, and completes the requests whose last task was in the wave.  New
+// requests join at every wave boundary, so their work overlaps on the device
+// with the running ones.  Waves are sized in time: after every wave the
+// scheduler knows each request's leaves per task so far (its counter / its
+// tasks run) and the device's leaves per second, and the next wave takes
+// about WAVE_SECONDS of work, so a request that arrives while deep ones run
+// waits a few milliseconds, not the length of a large wave.
 //
 // The reference has no serving path; its nearest caller is the host work
 // queue of perft_multi_threaded_gpu_launcher (launcher.h:476-583), which
@@ -38,6 +43,12 @@ namespace {
 
 constexpr int TASK_DEPTH = 5;               // remaining depth of one task
 constexpr u32 MAX_WAVE_TASKS = 1u << 16;
+#ifndef PG_WAVE_SECONDS
+#define PG_WAVE_SECONDS 0.004
+#endif
+constexpr double WAVE_SECONDS = PG_WAVE_SECONDS;  // target device time of one wave
+constexpr double MIN_WAVE_LEAVES = 1e9;     // floor of the timed wave budget
+constexpr double MAX_WAVE_LEAVES = 4e10;
 
 struct Segment {
     u64 src;    // first task in the pool (index in boards)
@@ -108,6 +119,8 @@ struct Request {
     u64 pool_off = 0, pool_len = 0;
     u32 ntasks = 0, next = 0;
     int task_depth = 0;
+    u64 acc_seen = 0;     // the request's counter after the last wave
+    double per_task = 0;  // measured leaves per task (0 until a wave ran)
 };
 
 // first-fit allocator over the frontier pool (units: boards)
@@ -162,7 +175,9 @@ struct Server {
     int slider = 0;
     bool use_tt = false;
     u64 tt_bytes = 0;
-    double wave_leaves = 4e9;
+    double wave_leaves = 4e9;  // fixed wave budget (max_wave_nodes) or the first wave's
+    bool timed_waves = true;   // size waves from the measured rate
+    double rate = 0;           // leaves per second over recent waves
     // device
     u64* acc = nullptr;
     Pos* pool = nullptr;
@@ -260,27 +275,43 @@ int run_wave(Server& S, std::unique_lock<std::mutex>& lk)
     Engine& E = engine();
     std::vector<Segment> segs;
     u32 total = 0;
-    const double share = S.wave_leaves / std::max<size_t>(1, S.active.size());
-    double budget = S.wave_leaves;
-    // pass 1: fair share per request; pass 2: the rest of the budget in admission order
-    for (int pass = 0; pass < 2 && total < MAX_WAVE_TASKS; pass++) {
-        for (u64 id : S.active) {
-            Request& r = S.reqs[id];
-            if (r.next >= r.ntasks || total >= MAX_WAVE_TASKS) continue;
-            const double per = est_leaves(r.task_depth);
-            const double allow = pass == 0 ? share : budget;
-            if (pass == 1 && budget <= 0) break;
-            u32 k = (u32)std::max(1.0, allow / per);
-            k = std::min(k, r.ntasks - r.next);
-            k = std::min(k, MAX_WAVE_TASKS - total);
-            if (pass == 1 && k == 0) continue;
-            segs.push_back(Segment{r.pool_off + r.next, k, total, (u32)r.slot, (u32)r.task_depth});
-            r.next += k;
-            total += k;
-            budget -= k * per;
-        }
+    const double wave_leaves =
+        (S.timed_waves && S.rate > 0)
+            ? std::min(MAX_WAVE_LEAVES, std::max(MIN_WAVE_LEAVES, S.rate * WAVE_SECONDS))
+            : S.wave_leaves;
+    // pass 1: one task of every active request, so none waits for a whole
+    // wave; pass 2: the rest of the budget by least remaining work first
+    // (a request's remaining tasks x its measured leaves per task), which
+    // keeps short requests from queueing behind long ones
+    double budget = wave_leaves;
+    std::vector<std::pair<double, u64>> order;
+    order.reserve(S.active.size());
+    for (u64 id : S.active) {
+        Request& r = S.reqs[id];
+        if (r.next >= r.ntasks || total >= MAX_WAVE_TASKS) continue;
+        const double per = r.per_task > 0 ? r.per_task : est_leaves(r.task_depth);
+        segs.push_back(Segment{r.pool_off + r.next, 1u, total, (u32)r.slot, (u32)r.task_depth});
+        r.next += 1;
+        total += 1;
+        budget -= per;
+        order.emplace_back(per * (r.ntasks - r.next), id);
+    }
+    std::sort(order.begin(), order.end());
+    for (const auto& o : order) {
+        if (budget <= 0 || total >= MAX_WAVE_TASKS) break;
+        Request& r = S.reqs[o.second];
+        if (r.next >= r.ntasks) continue;
+        const double per = r.per_task > 0 ? r.per_task : est_leaves(r.task_depth);
+        u32 k = (u32)std::min<double>(budget / per + 1.0, (double)(r.ntasks - r.next));
+        k = std::min(k, MAX_WAVE_TASKS - total);
+        if (k == 0) continue;
+        segs.push_back(Segment{r.pool_off + r.next, k, total, (u32)r.slot, (u32)r.task_depth});
+        r.next += k;
+        total += k;
+        budget -= k * per;
     }
     if (!total) return PG_OK;
+    const double t_wave = now_s();
     memcpy(S.seg_host, segs.data(), segs.size() * sizeof(Segment));
     SRV_CUDA(cudaMemcpyAsync(S.seg_dev, S.seg_host, segs.size() * sizeof(Segment), cudaMemcpyHostToDevice, E.stream));
     k_gather_wave<<<std::min<u32>((total + 255) / 256, 2048), 256, 0, E.stream>>>(S.pool, S.seg_dev, (u32)segs.size(),
@@ -314,6 +345,19 @@ int run_wave(Server& S, std::unique_lock<std::mutex>& lk)
     }
     lk.lock();
     S.waves++;
+    if (st == PG_OK) {
+        // measured leaves per task of every request and the device's rate
+        double got = 0;
+        for (u64 id : S.active) {
+            Request& r = S.reqs[id];
+            const u64 a = S.acc_host[r.slot];
+            got += (double)(a - r.acc_seen);
+            r.acc_seen = a;
+            if (r.next) r.per_task = std::max(1.0, (double)a / r.next);
+        }
+        const double dt = now_s() - t_wave;
+        if (dt > 0 && got > 0) S.rate = S.rate > 0 ? 0.5 * S.rate + 0.5 * got / dt : got / dt;
+    }
     // completions
     std::vector<u64> still;
     for (u64 id : S.active) {
@@ -394,7 +438,10 @@ int pg_server_start(const pg_server_config* cfg)
     S->slider = cfg ? cfg->slider : 0;
     S->use_tt = cfg && cfg->use_tt;
     S->tt_bytes = cfg ? cfg->tt_bytes : 0;
-    if (cfg && cfg->max_wave_nodes) S->wave_leaves = (double)cfg->max_wave_nodes * est_leaves(TASK_DEPTH);
+    if (cfg && cfg->max_wave_nodes) {
+        S->wave_leaves = (double)cfg->max_wave_nodes * est_leaves(TASK_DEPTH);
+        S->timed_waves = false;
+    }
     const u64 budget = (cfg && cfg->hbm_budget_bytes) ? cfg->hbm_budget_bytes : (2ull << 30);
     S->pool_cap = budget / sizeof(Pos);
     cudaError_t e = cudaSetDevice(E.device);
