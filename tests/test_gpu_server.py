@@ -76,3 +76,29 @@ def test_server_with_tt_matches_golden_and_repeats(pg):
     finally:
         srv.stop()
         pg.tt_clear()
+
+
+def test_short_request_overtakes_running_deep_one(pg):
+    """A short request submitted while a deep one runs is admitted at the next
+    wave boundary and finishes long before the deep one (waves are a few
+    milliseconds of work, filled by least remaining work first)."""
+    g2 = golden_json("config2.json")
+    fens = {f["name"]: f for f in golden_json("fens.json")}
+    deep = pg.HexaBitBoardPosition(*words_of_hex(g2["board"]))
+    pos2 = pg.board_from_fen(fens["position2"]["fen"])
+    assert pg.perft(deep, 5) > 0                              # autotuner and tables ready
+    srv = pg.Server(hbm_budget_bytes=1 << 30, max_inflight=16)
+    try:
+        t_deep = time.perf_counter()
+        rid_deep = srv.submit(deep, 7)                        # 8.7e10 leaves
+        time.sleep(0.005)
+        t_short = time.perf_counter()
+        rid_short = srv.submit(pos2, 4)
+        n_short, lat_short = srv.wait(rid_short, timeout=300)
+        n_deep, lat_deep = srv.wait(rid_deep, timeout=300)
+    finally:
+        srv.stop()
+    assert n_short == fens["position2"]["perft"]["4"]
+    assert n_deep == g2["perft7"]
+    # completion times on the host clock: the short one first, by a margin
+    assert t_short + lat_short / 1e3 < t_deep + lat_deep / 1e3 - 0.02, (lat_short, lat_deep)
