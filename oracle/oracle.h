@@ -1,8 +1,8 @@
 /*
  * oracle.h -- CPU restatement of the reference perft move generator.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker that the GPU engine
- * is compared against.  It is loaded by tests/, by __graft_entry__.smoke() and
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle that the GPU engine's
+ * counts are compared against.  It is loaded by tests/, by __graft_entry__.smoke() and
  * by bench.py's CPU-baseline / reference leg, and by nothing else.  The product
  * (perft_gpu_gb300/) never links, loads or calls it.
  *
