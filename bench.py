@@ -18,7 +18,13 @@ against tests/golden/config3.npz (the reference's own CPU counts).
 
 --impl reference times the reference's CPU perft on the host cores instead:
 oracle/_ref (the reference compiled from its sources) where it was built,
-else the oracle's C restatement of it.
+else the oracle's C restatement of it, on the same fixed sample of the
+workload every step (every 16th position, the sample of the cpu_baseline leg).
+
+--profile-case N runs every (4096/N)-th position of the workload once
+(Kogge-Stone sliders, 128-thread CTAs, two-ply leaf: the autotuner's choice
+for the depths that hold most leaves), checks the counts and prints one JSON
+line: the small case of the same kernels for ncu captures.
 """
 from __future__ import annotations
 
@@ -176,6 +182,13 @@ def cpu_leaves_per_s(boards, depths, threads, prefer_reference=True):
     return out, secs, kind
 
 
+def config_of(n, leaves_per_step, slider, world):
+    """The workload description shared by both arms' JSON lines."""
+    return {"workload": WORKLOAD_NAME, "positions": n, "leaves_per_step": leaves_per_step, "slider": slider,
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "256 MiB buffer rewritten before every step (inside the timed region)"}
+
+
 def run_reference(args):
     world, rank, local, dist = dist_setup()
     if rank != 0:
@@ -197,8 +210,8 @@ def run_reference(args):
     leaves = 0
     secs = 0.0
     kind = None
+    idx = np.arange(0, len(boards), stride)  # the same sample every step
     for step in range(args.warmup + args.steps):
-        idx = np.arange(step % stride, len(boards), stride)
         out, s, kind = cpu_leaves_per_s(boards[idx], depths[idx], threads)
         if totals is not None and not np.array_equal(out, totals[idx]):
             print(json.dumps({"impl": "reference", "error": "CPU counts differ from golden"}))
@@ -212,12 +225,12 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded playouts, same positions as the GPU arm)",
-        "config": {"workload": WORKLOAD_NAME, "positions": len(boards),
-                   "sample": "each step: positions i = step (mod %d)" % stride},
+        "config": config_of(len(boards), int(totals.sum()) if totals is not None else None, args.slider, world),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "leaf nodes/s", "cores": threads, "kind": kind,
                          "cpu_model": cpu_model(),
-                         "sample": "1/%d of the 4096 positions per step (%d steps)" % (stride, args.steps)},
+                         "sample": "every %dth of the 4096 positions, the same %d positions (%d leaves) every "
+                                   "step, each timed whole" % (stride, len(idx), int(out.sum()))},
         "e2e": {"value": value, "unit": "leaf nodes/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -596,10 +609,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (seeded random legal playouts made on the GPU; counts verified "
                     "against the reference's golden counts)" if verified else "synthetic",
-            "config": {"workload": WORKLOAD_NAME, "positions": n,
-                       "leaves_per_step": leaves_per_step, "slider": slider,
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "256 MiB buffer rewritten before every step (inside the timed region)"},
+            "config": config_of(n, leaves_per_step, slider, world),
             "verified_bit_exact": verified,
             "e2e": {"value": e2e_value, "unit": "leaf nodes/s",
                     "h2d_bytes_per_step": n * 48 + n, "d2h_bytes_per_step": n * 8},
@@ -633,6 +643,27 @@ def run_ours(args):
     return 0
 
 
+def run_profile_case(args):
+    """One pass over a subset of the batched workload, for ncu captures."""
+    import perft_gpu_gb300 as pg
+    pg.load_library(build_if_missing=True)
+    pg.init()
+    g = golden_totals()
+    boards, depths = pg.random_playouts(WORKLOAD["seed"], WORKLOAD["n"], WORKLOAD["min_plies"],
+                                        WORKLOAD["max_plies"], WORKLOAD["min_moves"],
+                                        WORKLOAD["depth_lo"], WORKLOAD["depth_hi"], with_depths=True)
+    idx = np.arange(0, len(boards), max(1, len(boards) // args.profile_case))
+    st = pg.PgStats()
+    out = pg.perft_batch(boards[idx], depths[idx], slider="ks", block_size=128, leaf_plies=2, stats=st)
+    ok = bool(np.array_equal(out, g[0][idx])) if g is not None else None
+    print(json.dumps({"profile_case": len(idx), "positions": "every %dth of the batched workload" % (len(boards) // len(idx)),
+                      "leaves": int(out.sum()), "verified_bit_exact": ok,
+                      "leaf_kernel_launches": st.leaf_kernel_launches, "leaf_parent_nodes": st.leaf_parent_nodes,
+                      "leaf_kernel_ms": st.leaf_kernel_ms, "device_ms": st.device_ms, "launches": st.launches}))
+    pg.shutdown()
+    return 0 if ok is not False else 1
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -649,9 +680,13 @@ def main():
                     help="skip the other workloads (64 x depth 5, one position at depth 7, TT)")
     ap.add_argument("--serve-rates", default="25,50,100", help="Poisson request rates (req/s)")
     ap.add_argument("--serve-seconds", type=float, default=8.0)
+    ap.add_argument("--profile-case", type=int, default=0,
+                    help="run N positions of the workload once and exit (small case for ncu)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.profile_case:
+        return run_profile_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

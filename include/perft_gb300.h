@@ -60,6 +60,17 @@ typedef enum pg_slider {
     PG_SLIDER_HYBRID = 4     /* Kogge-Stone enemy fills, magic lookups for the king and own sliders */
 } pg_slider;
 
+/* pg_opts.use_tt.  PG_TT_ON: the per-depth HBM tables plus the in-level
+ * duplicate pass (the reference's perft_bb_gpu_simple_hash,
+ * perft_bb.h:1242-1589).  PG_TT_DEDUP_ONLY: the same driver with only the
+ * duplicate pass inside each level (no HBM tables: none allocated, probed or
+ * stored).  Counts are identical in every mode. */
+typedef enum pg_tt_mode {
+    PG_TT_OFF = 0,
+    PG_TT_ON = 1,
+    PG_TT_DEDUP_ONLY = 2
+} pg_tt_mode;
+
 typedef struct pg_config {
     int device;                  /* CUDA device ordinal (default 0) */
     uint64_t hbm_budget_bytes;   /* level buffers + TT; 0 = 60% of free HBM */
@@ -84,7 +95,7 @@ typedef struct pg_opts {
     int slider;                  /* pg_slider; PG_SLIDER_AUTO = tuned per call */
     int block_size;              /* leaf/expand CTA size: 0 = tuned, else 128/256/512 */
     int leaf_plies;              /* plies handled inside one CTA at the leaf: 0 = tuned, 1 or 2 */
-    int use_tt;                  /* transposition tables on (1) / off (0) */
+    int use_tt;                  /* pg_tt_mode: PG_TT_OFF, PG_TT_ON, PG_TT_DEDUP_ONLY */
     uint64_t tt_bytes;           /* total TT bytes across depths; 0 = from budget */
     int graph;                   /* replay the call's launch sequence from a captured CUDA graph */
     pg_stats *stats;             /* optional out */
@@ -140,14 +151,17 @@ int pg_perft_batch_device(const pg_board *d_pos, const uint8_t *d_depths, uint32
  * device array of 60 MiB that every GPU loading this library keeps until
  * the process exits, so the call makes no cudaMalloc, cudaFree or other
  * allocating call.  Limits: n <= 65536 positions, depths 0..3, and at most
- * 1,048,576 children of the depth-3 positions; larger requests return
- * PG_ERR_CAPACITY before any work.  The first call on a device looks up the
- * array's device address and uploads the move tables (about 0.9 MB, into
- * file-scope device arrays of this library); make that first call
- * before any stream capture.  stream may be NULL (the default stream); the
- * call returns when d_out is written.  Every call reuses the same array, so
- * calls that overlap on the GPU (other threads, other streams) race.  Does
- * not need pg_init. */
+ * 1,048,576 children of the depth-3 positions per call (both sides to move
+ * together).  Larger requests return PG_ERR_CAPACITY; every size check is
+ * made before the counting kernels, so d_out then holds zeros.  The first
+ * call on a device uploads the move tables (about 0.9 MB, into file-scope
+ * device arrays of this library); make that first call before any stream
+ * capture.  Every call looks up the array's device address again (no
+ * allocation), and a call that finds the tables gone after a device reset
+ * uploads them again.  stream may be NULL (the default stream); the call
+ * synchronises it and returns when d_out is written.  Every call reuses the
+ * same array, so calls that overlap on the GPU (other threads, other
+ * streams) race.  Does not need pg_init. */
 int pg_perft_batch_noalloc(const pg_board *d_pos, const uint8_t *d_depths, uint32_t n,
                            uint64_t *d_out, void *stream);
 
@@ -170,6 +184,22 @@ int pg_autotune(pg_tuning *out);
  * entry stays valid for its position and remaining depth, so results never
  * depend on what earlier calls stored).  No counterpart in the reference. */
 int pg_tt_clear(void);
+
+/* The 128-bit Zobrist key the device tables use for a position
+ * (computeZobristKey128b, MoveGeneratorBitboard.h:3914-3980, and
+ * HashKey128b, chess.h:410-452, with this engine's seeded key set): key[0]
+ * is the low word (its low bits pick the table slot), key[1] the high word.
+ * The half-move clock is not part of the key.  Host code: needs no GPU and
+ * no pg_init. */
+int pg_zobrist_key(const pg_board *pos, uint64_t key[2]);
+/* The 32-byte table entry of a key and its count, and the check a probe
+ * makes (the reference's XOR-verified entries, chess.h:454-482 and the probe
+ * of perft_bb.h:690-693, widened to verify all 128 key bits):
+ * entry = {k0 ^ v, k1 ^ v, v, mix(k0, k1) ^ v}; pg_tt_entry_match sets
+ * *accepted to 1 and *count to v only when all three checks hold for key.
+ * Host code: needs no GPU and no pg_init. */
+int pg_tt_entry_pack(const uint64_t key[2], uint64_t count, uint64_t entry[4]);
+int pg_tt_entry_match(const uint64_t entry[4], const uint64_t key[2], int *accepted, uint64_t *count);
 
 /* Snapshot of the transposition tables on disk, so a later process starts
  * with the subtrees an earlier one counted (the reference's disk hash,
@@ -220,7 +250,7 @@ typedef struct pg_server_config {
     uint32_t max_wave_nodes;     /* fixed wave size in frontier nodes (positions 5 plies above the
                                     leaves); 0 = waves sized in time, about 4 ms of device work
                                     each from the measured rate and leaves per task */
-    int use_tt;                  /* count the waves through the transposition tables, which persist
+    int use_tt;                  /* pg_tt_mode of the waves; with PG_TT_ON the tables persist
                                     across requests (launcher.h:699-790 keeps its table across runs) */
     uint64_t tt_bytes;           /* TT size when use_tt; 0 = from the engine budget (as pg_opts) */
 } pg_server_config;

@@ -16,7 +16,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libperft_ref.so")
-REF_DIR_DEFAULT = "/root/reference"
+# the reference tree is looked for beside this repository unless REF_DIR names it
+REF_DIR_DEFAULT = os.environ.get("REF_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 BOARD_DTYPE = np.dtype([("white", "<u8"), ("pawns", "<u8"), ("knights", "<u8"),
                         ("bishop_queens", "<u8"), ("rook_queens", "<u8"), ("kings", "<u8")])

@@ -35,6 +35,9 @@ STATUS_NAMES = {0: "PG_OK", 1: "PG_ERR_NOT_INITIALIZED", 2: "PG_ERR_INVALID_ARGU
                 6: "PG_ERR_DEVICE_TIMEOUT", 7: "PG_ERR_BUSY", 8: "PG_ERR_CAPACITY"}
 
 SLIDER_AUTO, SLIDER_KOGGE_STONE, SLIDER_FANCY, SLIDER_BYTE_SMEM, SLIDER_HYBRID = 0, 1, 2, 3, 4
+# pg_tt_mode: use_tt=True is TT_ON; "dedup" (or TT_DEDUP_ONLY) runs the TT
+# driver with only the in-level duplicate pass (no HBM tables)
+TT_OFF, TT_ON, TT_DEDUP_ONLY = 0, 1, 2
 SLIDERS = {"auto": 0, "ks": 1, "fancy": 2, "byte": 3, "hybrid": 4}
 
 # CMove flags (chess.h:272-293)
@@ -164,6 +167,11 @@ _SIGNATURES = {
     "pg_autotune": [ctypes.POINTER(PgTuning)],
     "pg_perft_split": [_BP, ctypes.c_int, ctypes.c_int, _U16P, _U64P, _U32P, _OP],
     "pg_selftest": [ctypes.c_int],
+    "pg_zobrist_key": [_BP, _U64P],
+    "pg_tt_entry_pack": [_U64P, ctypes.c_uint64, _U64P],
+    "pg_tt_entry_match": [_U64P, _U64P, ctypes.POINTER(ctypes.c_int), _U64P],
+    "pg_perft_batch_noalloc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                               ctypes.c_void_p],
 }
 
 _lib = None
@@ -197,12 +205,20 @@ def _check(status: int):
         raise PerftError(status, load_library().pg_last_error().decode(errors="replace"))
 
 
+def _tt_mode(use_tt) -> int:
+    if isinstance(use_tt, str):
+        return {"off": TT_OFF, "on": TT_ON, "dedup": TT_DEDUP_ONLY}[use_tt]
+    if isinstance(use_tt, bool) or use_tt is None:
+        return TT_ON if use_tt else TT_OFF
+    return int(use_tt)
+
+
 def _opts(slider=None, block_size=0, use_tt=False, tt_bytes=0, graph=False, stats=None, leaf_plies=0):
     o = PgOpts()
     o.slider = SLIDERS[slider] if isinstance(slider, str) else (slider or 0)
     o.block_size = block_size
     o.leaf_plies = leaf_plies
-    o.use_tt = 1 if use_tt else 0
+    o.use_tt = _tt_mode(use_tt)
     o.tt_bytes = tt_bytes
     o.graph = 1 if graph else 0
     o.stats = ctypes.pointer(stats) if stats is not None else None
@@ -358,6 +374,31 @@ def tt_load(path: str):
     _check(load_library().pg_tt_load(os.fsencode(path)))
 
 
+def zobrist_key(pos: HexaBitBoardPosition) -> tuple[int, int]:
+    """The 128-bit Zobrist key (low word, high word) the device tables use."""
+    k = (ctypes.c_uint64 * 2)()
+    _check(load_library().pg_zobrist_key(ctypes.byref(pos), k))
+    return k[0], k[1]
+
+
+def tt_entry_pack(key: tuple[int, int], count: int) -> tuple[int, int, int, int]:
+    """The four 64-bit words of a table entry holding `count` for `key`."""
+    k = (ctypes.c_uint64 * 2)(*key)
+    e = (ctypes.c_uint64 * 4)()
+    _check(load_library().pg_tt_entry_pack(k, count, e))
+    return tuple(e)
+
+
+def tt_entry_match(entry, key: tuple[int, int]):
+    """The count a probe for `key` reads from `entry`, or None (a miss)."""
+    e = (ctypes.c_uint64 * 4)(*entry)
+    k = (ctypes.c_uint64 * 2)(*key)
+    acc = ctypes.c_int()
+    v = ctypes.c_uint64()
+    _check(load_library().pg_tt_entry_match(e, k, ctypes.byref(acc), ctypes.byref(v)))
+    return v.value if acc.value else None
+
+
 def board_of(row) -> HexaBitBoardPosition:
     return HexaBitBoardPosition(*(int(row[k]) for k in BOARD_DTYPE.names))
 
@@ -374,10 +415,10 @@ class Server:
     """Continuous-batching perft server (pg_server_*)."""
 
     def __init__(self, hbm_budget_bytes: int = 0, max_inflight: int = 0, slider: int | str = 0,
-                 max_wave_nodes: int = 0, use_tt: bool = False, tt_bytes: int = 0):
+                 max_wave_nodes: int = 0, use_tt: bool | int | str = False, tt_bytes: int = 0):
         cfg = PgServerConfig(hbm_budget_bytes, max_inflight,
                              SLIDERS[slider] if isinstance(slider, str) else slider, max_wave_nodes,
-                             1 if use_tt else 0, tt_bytes)
+                             _tt_mode(use_tt), tt_bytes)
         _check(load_library().pg_server_start(ctypes.byref(cfg)))
 
     def submit(self, pos: HexaBitBoardPosition, depth: int) -> int:

@@ -108,6 +108,7 @@ int launch_scan(const u32* cnt, u32 n, u64* offs)
     Engine& E = engine();
     const u64 tiles = (n + SCAN_TILE - 1) / SCAN_TILE + 1;
     if (tiles > E.scan_status_cap) {
+        E.alloc_gen++;
         if (E.scan_status) cudaFree(E.scan_status);
         E.scan_status = nullptr;
         E.scan_status_cap = 0;
@@ -153,6 +154,7 @@ int ensure_level(int L, u64 need)
     u64 cap = 1u << 16;
     while (cap < need) cap <<= 1;
     cap = std::min(cap, std::max(level_cap_max(), need));
+    E.alloc_gen++;
     if (lb.block) {
         PG_CUDA(cudaStreamSynchronize(E.stream));
         cudaFree(lb.block);
@@ -437,6 +439,15 @@ static bool valid_board(const pg_board& b)
     return true;
 }
 
+static int check_opts(const pg_opts* o)
+{
+    if (o && (o->use_tt < PG_TT_OFF || o->use_tt > PG_TT_DEDUP_ONLY)) {
+        set_error("use_tt %d is not a pg_tt_mode", o->use_tt);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    return PG_OK;
+}
+
 static int check_ready()
 {
     if (!engine().ready) {
@@ -450,6 +461,7 @@ int ensure_stage(u64 bytes)
 {
     Engine& E = engine();
     if (E.stage_cap >= bytes) return PG_OK;
+    E.alloc_gen++;
     if (E.stage) cudaFree(E.stage);
     E.stage = nullptr;
     E.stage_cap = 0;
@@ -555,8 +567,11 @@ static int perft_batch_graph_locked(const Pos* d_pos, const unsigned char* d_dep
     PG_CUDA(cudaStreamSynchronize(E.stream));
     const u64 sum = E.host_scratch[128];
     GraphCache& g = E.graph;
-    const bool hit = g.exec && g.pos == d_pos && g.dep == d_depths && g.out == d_out && g.n == n && g.sum == sum &&
-                     g.slider == v.slider && g.T == v.T && g.leaf_plies == v.leaf_plies && g.per_depth == v.per_depth;
+    // a graph names the level, scan and staging buffers of its capture: any
+    // reallocation since (alloc_gen) makes it stale, never replayed
+    const bool hit = g.exec && g.alloc_gen == E.alloc_gen && g.pos == d_pos && g.dep == d_depths && g.out == d_out &&
+                     g.n == n && g.sum == sum && g.slider == v.slider && g.T == v.T &&
+                     g.leaf_plies == v.leaf_plies && g.per_depth == v.per_depth;
     if (hit) {
         cudaEventRecord(E.ev0, E.stream);
         PG_CUDA(cudaGraphLaunch(g.exec, E.stream));
@@ -612,6 +627,7 @@ static int perft_batch_graph_locked(const Pos* d_pos, const unsigned char* d_dep
     g.leaf_plies = v.leaf_plies;
     g.per_depth = v.per_depth;
     g.launches = rec_stats.launches;
+    g.alloc_gen = E.alloc_gen;
     E.st.graph_captures = 1;
     return PG_OK;
 }
@@ -1098,6 +1114,7 @@ int pg_perft_split(const pg_board* pos, int depth, int split_plies, pg_move* mov
     Engine& E = engine();
     std::lock_guard<std::mutex> lk(E.mu);
     PG_TRY(check_ready());
+    PG_TRY(check_opts(opts));
     if (!valid_board(*pos)) {
         set_error("not a valid board");
         return PG_ERR_INVALID_POSITION;
@@ -1121,6 +1138,7 @@ int pg_selftest(int which)
         E.fail_next_alloc = true;
         // drop the level buffers so that the next call must allocate
         cudaStreamSynchronize(E.stream);
+        E.alloc_gen++;
         for (auto& lb : E.lv) {
             if (lb.block) cudaFree(lb.block);
             lb = LevelBuf{};
@@ -1171,6 +1189,7 @@ int pg_perft_batch_device(const pg_board* d_pos, const uint8_t* d_depths, uint32
     Engine& E = engine();
     std::lock_guard<std::mutex> lk(E.mu);
     PG_TRY(check_ready());
+    PG_TRY(check_opts(opts));
     if (n == 0) return PG_OK;
     PG_TRY(begin_call(opts));
     if (opts && opts->use_tt) {
@@ -1189,6 +1208,7 @@ int pg_perft_batch(const pg_board* pos, const uint8_t* depths, uint32_t n, uint6
     Engine& E = engine();
     std::unique_lock<std::mutex> lk(E.mu);
     PG_TRY(check_ready());
+    PG_TRY(check_opts(opts));
     if (n == 0) return PG_OK;
     for (u32 i = 0; i < n; i++) {
         if (!valid_board(pos[i])) { set_error("position %u is not a valid board", i); return PG_ERR_INVALID_POSITION; }

@@ -65,6 +65,7 @@ struct GraphCache {
     int slider = 0, T = 0, leaf_plies = 0;
     bool per_depth = false;
     u64 launches = 0;
+    u64 alloc_gen = 0;  // Engine::alloc_gen when captured
 };
 
 struct Engine {
@@ -104,6 +105,10 @@ struct Engine {
     size_t rec_next = 0;
     u32 rec_part[4] = {};
     GraphCache graph;
+    // bumped whenever a device buffer that a captured graph may name (level
+    // buffers, scan status words, the staging buffer) is freed or
+    // reallocated; a cached graph from an older generation is re-captured
+    u64 alloc_gen = 0;
     // statistics of the current call
     pg_stats st{};
     // autotuner result: best leaf variant per root depth, switch depth

@@ -173,7 +173,7 @@ struct Server {
     std::vector<int> free_slots;
     u32 max_inflight = 4096;
     int slider = 0;
-    bool use_tt = false;
+    int use_tt = PG_TT_OFF;  // pg_tt_mode of the waves
     u64 tt_bytes = 0;
     double wave_leaves = 4e9;  // fixed wave budget (max_wave_nodes) or the first wave's
     bool timed_waves = true;   // size waves from the measured rate
@@ -326,7 +326,7 @@ int run_wave(Server& S, std::unique_lock<std::mutex>& lk)
     o.slider = S.slider;
     int st;
     if (S.use_tt) {
-        o.use_tt = 1;
+        o.use_tt = S.use_tt;
         o.tt_bytes = S.tt_bytes;
         st = tt_perft_batch_device(S.wave_pos, S.wave_dep, total, S.task_out, &o);
         if (st == PG_OK) {
@@ -436,7 +436,12 @@ int pg_server_start(const pg_server_config* cfg)
     Server* S = new Server();
     S->max_inflight = (cfg && cfg->max_inflight) ? cfg->max_inflight : 4096;
     S->slider = cfg ? cfg->slider : 0;
-    S->use_tt = cfg && cfg->use_tt;
+    S->use_tt = cfg ? cfg->use_tt : PG_TT_OFF;
+    if (S->use_tt < PG_TT_OFF || S->use_tt > PG_TT_DEDUP_ONLY) {
+        delete S;
+        set_error("use_tt %d is not a pg_tt_mode", cfg->use_tt);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
     S->tt_bytes = cfg ? cfg->tt_bytes : 0;
     if (cfg && cfg->max_wave_nodes) {
         S->wave_leaves = (double)cfg->max_wave_nodes * est_leaves(TASK_DEPTH);

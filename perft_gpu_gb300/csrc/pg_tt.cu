@@ -4,18 +4,20 @@
 // entries chess.h:410-504; probes perft_bb.h:664-761; duplicate marking
 // perft_bb.h:790-852; upsweep and stores perft_bb.h:854-961) re-planned for
 // the chunked breadth-first driver:
-//   * keys: 781 seeded 64-bit Zobrist numbers (piece-square x 768, castling
-//     rights x 4, en-passant file x 8, side to move), a fresh seeded set
-//     rather than the reference's randoms.cpp (counts do not depend on keys);
-//   * one table per remaining depth 2..9, 16-byte entries {key ^ count,
-//     count} written with one 16-byte store and accepted only when the XOR of
-//     the two words equals the probing key, so a torn or foreign entry is a
-//     miss, never a wrong count (the reference's lockless XOR scheme);
+//   * keys: 128-bit Zobrist keys (pg_zobrist.cuh: two seeded 64-bit words
+//     per feature, the shape of the reference's HashKey128b);
+//   * one table per remaining depth 2..9 of 32-byte entries that carry the
+//     count XORed into all 128 key bits (pg_zobrist.cuh), written as two
+//     16-byte stores; a foreign or torn entry is a miss, never a wrong count
+//     (the reference's lockless XOR scheme, widened to the whole key);
 //   * per level: probe (a hit resolves the node), duplicate detection inside
-//     the level (first claim in a level table; later equal keys take the
-//     claimant's count), the usual leaf / count / scan / expand for the live
-//     nodes, and after each chunk an upsweep that stores the children's final
-//     counts and adds them into their parents.
+//     the level (first claim in a level table by a 64-bit digest; a later
+//     node takes the claimant's count only if its full 128-bit key and
+//     remaining depth are equal), the usual leaf / count / scan / expand for
+//     the live nodes, and after each chunk an upsweep that stores the
+//     children's final counts and adds them into their parents;
+//   * use_tt = 2 (PG_TT_DEDUP_ONLY) runs the same driver without the HBM
+//     tables: only the in-level duplicate pass.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,23 +28,26 @@
 #include "pg_kernels.cuh"
 #include "pg_tables.h"
 #include "pg_tt.cuh"
+#include "pg_zobrist.cuh"
 
 namespace pg {
 
-constexpr int ZOBRIST_KEYS = 781;
-constexpr int Z_CASTLE = 768, Z_EP = 772, Z_SIDE = 780;
 constexpr int TT_MIN_DEPTH = 2, TT_MAX_DEPTH = 9;
 constexpr u32 NO_DUP = 0xFFFFFFFFu;
+constexpr u64 TT_ENTRY_BYTES = 32;
 
-static __device__ u64 g_zobrist[ZOBRIST_KEYS];
+static __device__ ulonglong2 g_zobrist[ZOBRIST_KEYS];
 
+// tab[d]: the table of remaining depth d, two ulonglong2 per entry (entry i
+// at tab[d][2i], tab[d][2i + 1]); null when that depth has no table
 struct TTSet {
     ulonglong2* tab[16];
     u64 mask[16];
 };
 
 struct LevelTT {
-    u64* hash = nullptr;
+    u64* hash0 = nullptr;  // 128-bit key of each node, low / high word
+    u64* hash1 = nullptr;
     u64* acc = nullptr;
     u32* parent = nullptr;
     u32* dup = nullptr;
@@ -54,7 +59,8 @@ struct LevelTT {
 
 struct TTState {
     bool keys_ready = false;
-    TTSet set{};
+    TTSet set{};     // the HBM tables
+    TTSet active{};  // what the current call probes and stores: set, or none (PG_TT_DEDUP_ONLY)
     void* pool = nullptr;
     u64 pool_bytes = 0;
     LevelTT lv[MAX_LEVELS];
@@ -68,29 +74,10 @@ static TTState g_tt;
 // kernels
 // ---------------------------------------------------------------------------
 
-// z: the 781 keys (staged in shared memory by the caller)
-__device__ __forceinline__ u64 zobrist_hash(const Pos& b, const u64* z)
-{
-    const u64 pawns = b.p & INNER;
-    const u64 sets[6] = {pawns, b.n, b.bq & ~b.rq, b.rq & ~b.bq, b.bq & b.rq, b.k};
-    u64 h = 0;
-#pragma unroll
-    for (int t = 0; t < 6; t++) {
-        for (u64 s = sets[t] & b.w; s; s &= s - 1) h ^= z[t * 64 + lsb(s)];
-        for (u64 s = sets[t] & ~b.w; s; s &= s - 1) h ^= z[(6 + t) * 64 + lsb(s)];
-    }
-    const int wc = st_wc(b), bc = st_bc(b), ep = st_ep(b);
-    if (wc & 1) h ^= z[Z_CASTLE + 0];
-    if (wc & 2) h ^= z[Z_CASTLE + 1];
-    if (bc & 1) h ^= z[Z_CASTLE + 2];
-    if (bc & 2) h ^= z[Z_CASTLE + 3];
-    if (ep) h ^= z[Z_EP + ((ep - 1) & 7)];
-    if (st_side(b)) h ^= z[Z_SIDE];
-    return h ? h : 1;  // 0 marks an empty slot of the duplicate table
-}
-
-// the duplicate key includes the remaining depth: one level of a mixed-depth
-// batch can hold the same position at different depths
+// the duplicate table's 64-bit digest of (key, remaining depth): one level of
+// a mixed-depth batch can hold the same position at different depths.  The
+// digest only finds the slot and the claimant; equality is decided on the
+// full key and depth (k_tt_dedup).
 __device__ __forceinline__ u64 dd_key(u64 h, u32 rem)
 {
     const u64 k = h ^ (0x9E3779B97F4A7C15ull * (rem + 1));
@@ -112,10 +99,10 @@ __device__ __forceinline__ void block_count_add(u64* dst, u32 v)
     if (threadIdx.x == 0 && s_sum) atomicAdd(dst, (u64)s_sum);
 }
 
-// hash, TT probe, and first claim of the level's duplicate table
+// key, TT probe, and first claim of the level's duplicate table
 static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TTSet tt, u64 dd_mask, u64* counters)
 {
-    __shared__ u64 z[ZOBRIST_KEYS];
+    __shared__ ulonglong2 z[ZOBRIST_KEYS];
     for (int i = threadIdx.x; i < ZOBRIST_KEYS; i += blockDim.x) z[i] = g_zobrist[i];
     __syncthreads();
     u32 probes = 0, hits = 0;
@@ -125,19 +112,23 @@ static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TT
         lt.acc[idx] = 0;
         lt.dup[idx] = NO_DUP;
         if (rem < TT_MIN_DEPTH || rem >= REM_DEAD) continue;
-        const u64 h = zobrist_hash(load_board(lv, idx), z);
-        lt.hash[idx] = h;
+        const Pos b = load_board(lv, idx);
+        const ulonglong2 h = zobrist128(&b.w, z);
+        lt.hash0[idx] = h.x;
+        lt.hash1[idx] = h.y;
         if (rem <= TT_MAX_DEPTH && tt.tab[rem]) {
             probes++;
-            const ulonglong2 e = tt.tab[rem][h & tt.mask[rem]];
-            if ((e.x ^ e.y) == h) {
-                lt.acc[idx] = e.y;
+            const ulonglong2* e = tt.tab[rem] + 2 * (h.x & tt.mask[rem]);
+            const ulonglong2 ea = e[0], eb = e[1];
+            u64 v;
+            if (tt_match(ea, eb, h.x, h.y, v)) {
+                lt.acc[idx] = v;
                 lv.rem[idx] = REM_DEAD;
                 hits++;
                 continue;
             }
         }
-        const u64 k = dd_key(h, rem);
+        const u64 k = dd_key(h.x, rem);
         const u32 s = dd_slot(k, dd_mask);
         const u64 prev = atomicCAS(&lt.dd_hash[s], 0ull, k);
         if (prev == 0 || prev == k) atomicMin(&lt.dd_idx[s], idx);
@@ -146,19 +137,24 @@ static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TT
     block_count_add(&counters[1], hits);
 }
 
-// a node whose key was claimed first by another node of its level takes that
-// node's count later and does no work itself
+// a node whose position and remaining depth were claimed first by another
+// node of its level takes that node's count later and does no work itself.
+// The claimant of a slot is the lowest index among the nodes with the
+// slot's digest; a node whose full key or depth differs from the claimant's
+// (a digest collision) keeps its own work.  Claimants are never marked here,
+// so their depth and key are stable while others compare against them.
 static __global__ void k_tt_dedup(LevelView lv, u32 start, u32 n, LevelTT lt, u64 dd_mask)
 {
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const u32 idx = start + i;
         const u32 rem = lv.rem[idx];
         if (rem < TT_MIN_DEPTH || rem >= REM_DEAD) continue;
-        const u64 k = dd_key(lt.hash[idx], rem);
+        const u64 h0 = lt.hash0[idx];
+        const u64 k = dd_key(h0, rem);
         const u32 s = dd_slot(k, dd_mask);
         if (lt.dd_hash[s] == k) {
             const u32 rep = lt.dd_idx[s];
-            if (rep != idx) {
+            if (rep != idx && lt.hash0[rep] == h0 && lt.hash1[rep] == lt.hash1[idx] && lv.rem[rep] == rem) {
                 lt.dup[idx] = rep;
                 lv.rem[idx] = REM_DEAD;
             }
@@ -166,10 +162,13 @@ static __global__ void k_tt_dedup(LevelView lv, u32 start, u32 n, LevelTT lt, u6
     }
 }
 
-__device__ __forceinline__ void tt_store(const TTSet& tt, u32 rem, u64 h, u64 v)
+__device__ __forceinline__ void tt_store(const TTSet& tt, u32 rem, u64 h0, u64 h1, u64 v)
 {
-    // one 16-byte store: {key ^ count, count}
-    tt.tab[rem][h & tt.mask[rem]] = make_ulonglong2(h ^ v, v);
+    ulonglong2 a, b;
+    tt_pack(h0, h1, v, a, b);
+    ulonglong2* e = tt.tab[rem] + 2 * (h0 & tt.mask[rem]);
+    e[0] = a;
+    e[1] = b;
 }
 
 // children [0, m) of one chunk are final: store them and add them to parents.
@@ -194,7 +193,7 @@ static __global__ void k_tt_upsweep(LevelView ch, u32 m, LevelTT ct, TTSet tt, u
             v = d != NO_DUP ? ct.acc[d] : ct.acc[j];
             const u32 rem = ch.rem[j];
             if (rem >= TT_MIN_DEPTH && rem <= TT_MAX_DEPTH && tt.tab[rem]) {
-                tt_store(tt, rem, ct.hash[j], v);
+                tt_store(tt, rem, ct.hash0[j], ct.hash1[j], v);
                 stores++;
             }
             par = ct.parent[j];
@@ -233,7 +232,7 @@ static __global__ void k_tt_finish(LevelView lv, u32 n, LevelTT lt, TTSet tt, co
         const u64 v = d != NO_DUP ? lt.acc[d] : lt.acc[s];
         const u32 rem = lv.rem[s];
         if (rem >= TT_MIN_DEPTH && rem <= TT_MAX_DEPTH && tt.tab[rem]) {
-            tt_store(tt, rem, lt.hash[s], v);
+            tt_store(tt, rem, lt.hash0[s], lt.hash1[s], v);
             stores++;
         }
         out[root_of[s]] = v;
@@ -261,19 +260,10 @@ static __global__ void k_tt_finish(LevelView lv, u32 n, LevelTT lt, TTSet tt, co
 
 static int small_grid(u64 n) { return (int)std::max<u64>(1, std::min<u64>((n + 255) / 256, 8192)); }
 
-constexpr u64 ZOBRIST_SEED = 0x5EED2B1D0C0FFEE5ull;
-
 int tt_upload_keys()
 {
-    // 781 keys from splitmix64 with a fixed seed
-    u64 keys[ZOBRIST_KEYS];
-    u64 s = ZOBRIST_SEED;
-    for (int i = 0; i < ZOBRIST_KEYS; i++) {
-        u64 z = (s += 0x9E3779B97F4A7C15ull);
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-        keys[i] = z ^ (z >> 31);
-    }
+    ulonglong2 keys[ZOBRIST_KEYS];
+    zobrist_key_table(keys);
     TT_CUDA(cudaMemcpyToSymbol(g_zobrist, keys, sizeof(keys)));
     const HostTables* t = host_tables();
     if (!t) {
@@ -296,16 +286,16 @@ static int ensure_tables(u64 bytes)
     }
     const int ntab = TT_MAX_DEPTH - TT_MIN_DEPTH + 1;
     u64 entries = 1;
-    while (entries * 2 * 16 * ntab <= bytes) entries *= 2;
+    while (entries * 2 * TT_ENTRY_BYTES * ntab <= bytes) entries *= 2;
     if (entries < 1024) {
         set_error("transposition-table budget of %llu bytes is too small", (unsigned long long)bytes);
         return PG_ERR_INVALID_ARGUMENT;
     }
-    TT_CUDA(cudaMalloc(&g_tt.pool, entries * 16 * ntab));
-    TT_CUDA(cudaMemsetAsync(g_tt.pool, 0, entries * 16 * ntab, E.stream));
+    TT_CUDA(cudaMalloc(&g_tt.pool, entries * TT_ENTRY_BYTES * ntab));
+    TT_CUDA(cudaMemsetAsync(g_tt.pool, 0, entries * TT_ENTRY_BYTES * ntab, E.stream));
     g_tt.pool_bytes = bytes;
     for (int d = TT_MIN_DEPTH; d <= TT_MAX_DEPTH; d++) {
-        g_tt.set.tab[d] = (ulonglong2*)g_tt.pool + (u64)(d - TT_MIN_DEPTH) * entries;
+        g_tt.set.tab[d] = (ulonglong2*)g_tt.pool + (u64)(d - TT_MIN_DEPTH) * entries * 2;
         g_tt.set.mask[d] = entries - 1;
     }
     if (!g_tt.counters) TT_CUDA(cudaMalloc(&g_tt.counters, 4 * sizeof(u64)));
@@ -324,7 +314,7 @@ static int ensure_level_tt(int L, u64 need)
     u64 cap = 1 << 16;
     while (cap < need) cap <<= 1;
     const u64 dd = cap * 2;
-    const u64 bytes = cap * (8 + 8 + 4 + 4) + dd * (8 + 4) + 1024;
+    const u64 bytes = cap * (8 + 8 + 8 + 4 + 4) + dd * (8 + 4) + 1024;
     void* blk = nullptr;
     cudaError_t e = cudaMalloc(&blk, bytes);
     if (e != cudaSuccess) {
@@ -334,7 +324,9 @@ static int ensure_level_tt(int L, u64 need)
         return PG_ERR_OUT_OF_MEMORY;
     }
     unsigned char* p = (unsigned char*)blk;
-    t.hash = (u64*)p;
+    t.hash0 = (u64*)p;
+    p += cap * 8;
+    t.hash1 = (u64*)p;
     p += cap * 8;
     t.acc = (u64*)p;
     p += cap * 8;
@@ -362,7 +354,7 @@ static int run_range_tt(const Variant& v, int L, u32 start, u32 n, int side, int
     dd = std::min(dd, lt.dd_cap);
     TT_CUDA(cudaMemsetAsync(lt.dd_hash, 0, dd * 8, E.stream));
     TT_CUDA(cudaMemsetAsync(lt.dd_idx, 0xFF, dd * 4, E.stream));
-    k_tt_probe<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, g_tt.set, dd - 1, g_tt.counters);
+    k_tt_probe<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, g_tt.active, dd - 1, g_tt.counters);
     k_tt_dedup<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, dd - 1);
     TT_CUDA(cudaGetLastError());
     E.st.launches += 2;
@@ -402,7 +394,7 @@ static int run_range_tt(const Variant& v, int L, u32 start, u32 n, int side, int
         E.st.launches++;
         TT_TRY(run_range_tt(v, L + 1, 0, (u32)children, 1 - side, cminrem, cmaxrem));
         k_tt_upsweep<<<small_grid(children), 256, 0, E.stream>>>(E.lv[L + 1].v, (u32)children, g_tt.lv[L + 1],
-                                                                 g_tt.set, lt.acc, g_tt.counters);
+                                                                 g_tt.active, lt.acc, g_tt.counters);
         TT_CUDA(cudaGetLastError());
         E.st.launches++;
     }
@@ -426,18 +418,19 @@ void tt_free()
 // file and probes it during the search (diskTTProbe, launcher.h:699-790, off
 // by default); here the HBM tables are written out whole and read back, so a
 // later process starts with the subtrees an earlier one counted.  The file is
-// a header (format, Zobrist seed, depth range, entries per table, the TT size
-// the tables were made for) followed by the tables as they lie in HBM.
+// a header (format, Zobrist seeds, depth range, entries per table, the TT
+// size the tables were made for) followed by the tables as they lie in HBM.
 // ---------------------------------------------------------------------------
 
 struct TTFileHeader {
     char magic[8];       // "PGTT" and the format version
-    u64 key_seed;        // entries are only valid under the same keys
+    u64 key_seed[2];     // entries are only valid under the same keys
     u32 min_depth, max_depth;
     u64 entries;         // per table (a power of two)
     u64 budget_bytes;    // the TT size the tables were made for
 };
-static const char TT_MAGIC[8] = {'P', 'G', 'T', 'T', 0, 0, 0, 1};
+// format 2: 128-bit keys, 32-byte entries
+static const char TT_MAGIC[8] = {'P', 'G', 'T', 'T', 0, 0, 0, 2};
 constexpr u64 TT_FILE_CHUNK = 64ull << 20;
 
 int tt_save(const char* path)
@@ -451,12 +444,13 @@ int tt_save(const char* path)
     const int ntab = TT_MAX_DEPTH - TT_MIN_DEPTH + 1;
     TTFileHeader h{};
     memcpy(h.magic, TT_MAGIC, sizeof(h.magic));
-    h.key_seed = ZOBRIST_SEED;
+    h.key_seed[0] = ZOBRIST_SEED0;
+    h.key_seed[1] = ZOBRIST_SEED1;
     h.min_depth = TT_MIN_DEPTH;
     h.max_depth = TT_MAX_DEPTH;
     h.entries = g_tt.set.mask[TT_MIN_DEPTH] + 1;
     h.budget_bytes = g_tt.pool_bytes;
-    const u64 total = h.entries * 16 * ntab;
+    const u64 total = h.entries * TT_ENTRY_BYTES * ntab;
     FILE* f = fopen(path, "wb");
     if (!f) {
         set_error("cannot open %s for writing", path);
@@ -496,7 +490,7 @@ int tt_load(const char* path)
     TTFileHeader h{};
     const int ntab = TT_MAX_DEPTH - TT_MIN_DEPTH + 1;
     if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, TT_MAGIC, sizeof(h.magic)) != 0 ||
-        h.key_seed != ZOBRIST_SEED || h.min_depth != (u32)TT_MIN_DEPTH || h.max_depth != (u32)TT_MAX_DEPTH ||
+        h.key_seed[0] != ZOBRIST_SEED0 || h.key_seed[1] != ZOBRIST_SEED1 || h.min_depth != (u32)TT_MIN_DEPTH || h.max_depth != (u32)TT_MAX_DEPTH ||
         h.entries < 1024 || (h.entries & (h.entries - 1))) {
         fclose(f);
         set_error("%s is not a transposition-table snapshot of this engine", path);
@@ -523,7 +517,7 @@ int tt_load(const char* path)
         set_error("cudaStreamSynchronize failed: %s", cudaGetErrorString(se));
         return PG_ERR_CUDA;
     }
-    const u64 total = h.entries * 16 * ntab;
+    const u64 total = h.entries * TT_ENTRY_BYTES * ntab;
     std::vector<unsigned char> buf((size_t)std::min(total, TT_FILE_CHUNK));
     for (u64 off = 0; off < total; off += TT_FILE_CHUNK) {
         const u64 len = std::min(TT_FILE_CHUNK, total - off);
@@ -553,7 +547,7 @@ int tt_clear()
 {
     Engine& E = engine();
     if (g_tt.pool) {
-        const u64 bytes = (g_tt.set.mask[TT_MIN_DEPTH] + 1) * 16ull * (TT_MAX_DEPTH - TT_MIN_DEPTH + 1);
+        const u64 bytes = (g_tt.set.mask[TT_MIN_DEPTH] + 1) * TT_ENTRY_BYTES * (TT_MAX_DEPTH - TT_MIN_DEPTH + 1);
         TT_CUDA(cudaMemsetAsync(g_tt.pool, 0, bytes, E.stream));
     }
     TT_CUDA(cudaStreamSynchronize(E.stream));
@@ -564,8 +558,15 @@ int tt_perft_batch_device(const Pos* d_pos, const unsigned char* d_depths, u32 n
 {
     Engine& E = engine();
     if (!g_tt.keys_ready) TT_TRY(tt_upload_keys());
-    u64 bytes = (o && o->tt_bytes) ? o->tt_bytes : std::min<u64>(32ull << 30, E.budget / 4);
-    TT_TRY(ensure_tables(bytes));
+    const bool tables = !(o && o->use_tt == PG_TT_DEDUP_ONLY);
+    if (tables) {
+        const u64 bytes = (o && o->tt_bytes) ? o->tt_bytes : std::min<u64>(32ull << 30, E.budget / 4);
+        TT_TRY(ensure_tables(bytes));
+        g_tt.active = g_tt.set;
+    } else {
+        g_tt.active = TTSet{};
+    }
+    if (!g_tt.counters) TT_CUDA(cudaMalloc(&g_tt.counters, 4 * sizeof(u64)));
     Variant v = pick_variant(o);
     v.leaf_plies = 2;  // the TT driver finishes the last two plies in the leaf kernel
     TT_TRY(ensure_level(0, n));
@@ -594,7 +595,7 @@ int tt_perft_batch_device(const Pos* d_pos, const unsigned char* d_depths, u32 n
     cudaEventRecord(E.ev0, E.stream);
     TT_TRY(run_range_tt(v, 0, 0, nw, 0, (int)mind, (int)maxd));
     TT_TRY(run_range_tt(v, 0, nw, n - nw, 1, (int)mind, (int)maxd));
-    k_tt_finish<<<small_grid(n), 256, 0, E.stream>>>(E.lv[0].v, n, g_tt.lv[0], g_tt.set, g_tt.root_of, d_out,
+    k_tt_finish<<<small_grid(n), 256, 0, E.stream>>>(E.lv[0].v, n, g_tt.lv[0], g_tt.active, g_tt.root_of, d_out,
                                                      g_tt.counters);
     TT_CUDA(cudaGetLastError());
     cudaEventRecord(E.ev1, E.stream);
@@ -612,3 +613,60 @@ int tt_perft_batch_device(const Pos* d_pos, const unsigned char* d_depths, u32 n
 }
 
 }  // namespace pg
+
+// ===========================================================================
+// C ABI: host-side key and entry helpers (the same inline code the kernels
+// run; no GPU needed)
+// ===========================================================================
+
+using namespace pg;
+
+extern "C" {
+
+int pg_zobrist_key(const pg_board* pos, uint64_t key[2])
+{
+    if (!pos || !key) {
+        set_error("null argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    static ulonglong2 keys[ZOBRIST_KEYS];
+    static const bool made = (zobrist_key_table(keys), true);
+    (void)made;
+    u64 w[6];
+    memcpy(w, pos, sizeof(w));
+    const ulonglong2 h = zobrist128(w, keys);
+    key[0] = h.x;
+    key[1] = h.y;
+    return PG_OK;
+}
+
+int pg_tt_entry_pack(const uint64_t key[2], uint64_t count, uint64_t entry[4])
+{
+    if (!key || !entry) {
+        set_error("null argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    ulonglong2 a, b;
+    tt_pack(key[0], key[1], count, a, b);
+    entry[0] = a.x;
+    entry[1] = a.y;
+    entry[2] = b.x;
+    entry[3] = b.y;
+    return PG_OK;
+}
+
+int pg_tt_entry_match(const uint64_t entry[4], const uint64_t key[2], int* accepted, uint64_t* count)
+{
+    if (!entry || !key || !accepted) {
+        set_error("null argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    u64 v = 0;
+    const bool ok = tt_match(make_ulonglong2(entry[0], entry[1]), make_ulonglong2(entry[2], entry[3]), key[0],
+                             key[1], v);
+    *accepted = ok ? 1 : 0;
+    if (count) *count = ok ? v : 0;
+    return PG_OK;
+}
+
+}  // extern "C"

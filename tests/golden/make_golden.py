@@ -1,7 +1,7 @@
 """Generates the golden vectors in tests/golden/ from the reference itself.
 
-Run in a container that holds the reference sources (REF_DIR, default
-/root/reference) on an x86-64 host:
+Run where the reference sources are present (REF_DIR, default the directory
+"reference" beside this repository):
 
     python tests/golden/make_golden.py            # all fixtures
     python tests/golden/make_golden.py fens walk  # a subset

@@ -157,3 +157,32 @@ def test_graph_capture_and_replay(pg):
     st = pg.PgStats()
     out2 = pg.perft_batch(b2, g["depths"][other], graph=True, stats=st)
     assert np.array_equal(out2, g["totals"][other]) and st.graph_captures == 1
+
+
+def test_graph_recaptured_after_buffers_are_reallocated(pg):
+    """A captured graph names the engine's level and scan buffers.  A later
+    call that grows those buffers (here: a batch with a much larger first
+    level) frees the ones the graph was captured with, so the next graph call
+    on the same inputs must capture again, never replay into freed memory."""
+    import torch
+    pg.shutdown()
+    pg.init()
+    g = golden_npz("config3.npz")
+    idx = np.arange(0, 4096, 11)
+    d_b = torch.from_numpy(g["boards"][idx].copy().view(np.uint8)).cuda()
+    d_d = torch.from_numpy(g["depths"][idx].copy()).cuda()
+    d_o = torch.zeros(len(idx), dtype=torch.int64, device="cuda")
+
+    def graph_call():
+        st = pg.PgStats()
+        pg.perft_batch_device(d_b.data_ptr(), d_d.data_ptr(), len(idx), d_o.data_ptr(), slider="ks",
+                              graph=True, stats=st)
+        assert np.array_equal(d_o.cpu().numpy().view(np.uint64), g["totals"][idx])
+        return st.graph_captures, st.graph_replays
+
+    assert graph_call() == (1, 0)
+    assert graph_call() == (0, 1)
+    big, big_d = pg.random_playouts(31, 20000, 0, 40, 1, 3, 3, with_depths=True)
+    assert pg.perft_batch(big, big_d, slider="ks").sum() > 0
+    assert graph_call() == (1, 0)
+    assert graph_call() == (0, 1)

@@ -89,3 +89,32 @@ def test_tt_snapshot_save_load(pg, tmp_path):
     with pytest.raises(pg.PerftError):
         pg.tt_load(str(tmp_path / "missing.snap"))
     pg.tt_clear()
+
+
+def test_tt_dedup_only_mode(pg):
+    """use_tt="dedup": the TT driver with only the in-level duplicate pass;
+    no table is probed or stored, counts are unchanged."""
+    g = golden_npz("config4_d5.npz")
+    boards = g["boards"].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    st = pg.PgStats()
+    out = pg.perft_batch(boards, [5] * len(boards), use_tt="dedup", stats=st)
+    assert np.array_equal(out, g["totals"])
+    assert st.tt_probes == 0 and st.tt_hits == 0 and st.tt_stores == 0
+    fens = {f["name"]: f for f in golden_json("fens.json")}
+    b = pg.board_from_fen(fens["position2"]["fen"])
+    assert pg.perft(b, 5, use_tt="dedup") == fens["position2"]["perft"]["5"]
+    with pytest.raises(pg.PerftError):
+        pg.perft(b, 3, use_tt=7)
+
+
+def test_tt_full_key_separates_positions_in_one_level(pg):
+    """Many distinct positions at one level with a tiny table (1 MB, constant
+    overwrites) and duplicates of each: every count equals the no-TT count."""
+    boards, depths = pg.random_playouts(41, 3000, 0, 60, 1, 3, 5, with_depths=True)
+    boards = np.concatenate([boards, boards[::3]])
+    depths = np.concatenate([depths, depths[::3]])
+    pg.tt_clear()
+    ref = pg.perft_batch(boards, depths)
+    for _ in range(2):
+        assert np.array_equal(pg.perft_batch(boards, depths, use_tt=True, tt_bytes=1 << 20), ref)
+    pg.tt_clear()
