@@ -263,7 +263,8 @@ def serve_leg(pg, rates, seconds, plain_rate):
     max_n = int(max(rates + [plain_rate]) * seconds * 1.5) + 64
     boards, depths, rng = serve_requests(pg, max_n)
     out = {"requests": "seeded playout positions (0-60 plies), depth lognormal(median 4, sigma 0.25) "
-                       "clipped to 3..8; Poisson arrivals", "rates": []}
+                       "clipped to 3..8; Poisson arrivals", "rates": [],
+           "stable_def": "completions per second >= 95% of the offered rate over the run"}
     check_n = 0
     for rate in rates:
         arrivals = np.cumsum(rng.exponential(1.0 / rate, max_n))
@@ -287,7 +288,11 @@ def serve_leg(pg, rates, seconds, plain_rate):
         check_n += n
         out["rates"].append({"rate_req_s": rate, "requests": n, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
                              "max_ms": max(lat) if lat else None, "leaves_per_s": leaves / wall,
-                             "completed_per_s": n / wall})
+                             "completed_per_s": n / wall, "stable": n / wall >= 0.95 * rate})
+    stable = [r for r in out["rates"] if r["stable"]]
+    if stable:
+        top = max(stable, key=lambda r: r["rate_req_s"])
+        out["highest_sustained"] = {"rate_req_s": top["rate_req_s"], "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"]}
     # the same kind of stream at the middle rate, served through the
     # transposition tables (they persist across requests)
     arrivals = np.cumsum(rng.exponential(1.0 / plain_rate, max_n))
@@ -404,32 +409,37 @@ def workloads_leg(pg, threads):
                                "readme_gtx780_leaves_per_s": 27e9,
                                "note": "README figure is one overclocked GTX 780 (Kepler); not the same hardware"}
 
-    # transposition-table workload: TT counts equal the no-TT counts
+    # transposition-table workload: TT counts equal the no-TT counts.  Modes:
+    # tables + in-level duplicate pass (use_tt=True), the duplicate pass alone
+    # (use_tt="dedup"), no TT; and the tables' second call on the same
+    # positions (warm tables: what they buy across calls and requests)
+    def tt_row(run, leaves_of):
+        rows = {}
+        pg.tt_clear()
+        for mode, kw in (("tables", {"use_tt": True}), ("tables_warm", {"use_tt": True}),
+                         ("dedup_only", {"use_tt": "dedup"}), ("no_tt", {})):
+            st = pg.PgStats()
+            r, secs = _timed(lambda: run(stats=st, **kw))
+            rows[mode] = {"seconds": secs, "device_ms": st.device_ms, "leaves": leaves_of(r)}
+            if kw.get("use_tt") is True:
+                rows[mode].update({"tt_probes": st.tt_probes, "tt_hits": st.tt_hits, "tt_stores": st.tt_stores,
+                                   "hit_rate": st.tt_hits / st.tt_probes if st.tt_probes else None,
+                                   "tt_entry_gb_per_s": (st.tt_probes + st.tt_stores) * 32 / (st.device_ms / 1e3)
+                                   / 1e9 if st.device_ms else None})
+        assert len({v["leaves"] for v in rows.values()}) == 1, rows
+        for v in rows.values():
+            v["speedup_vs_no_tt"] = rows["no_tt"]["seconds"] / v["seconds"]
+        pg.tt_clear()
+        return rows
+
     tt = {}
-    pg.tt_clear()
-    st = pg.PgStats()
-    r_tt, s_tt = _timed(lambda: pg.perft(b2, 8, use_tt=True, stats=st))
-    st0 = pg.PgStats()
-    r_no, s_no = _timed(lambda: pg.perft(b2, 8, stats=st0))
-    assert r_tt == r_no
-    tt["position_depth8"] = {"leaves": r_tt, "tt_s": s_tt, "no_tt_s": s_no, "speedup": s_no / s_tt,
-                             "tt_probes": st.tt_probes, "tt_hits": st.tt_hits, "tt_stores": st.tt_stores,
-                             "tt_entry_gb_per_s": (st.tt_probes + st.tt_stores) * 16 / (st.device_ms / 1e3) / 1e9
-                             if st.device_ms else None}
+    tt["position_depth8"] = tt_row(lambda **kw: pg.perft(b2, 8, **kw), lambda r: int(r))
     c4 = np.load(os.path.join(ROOT, "tests", "golden", "config4_d5.npz"))
     b4 = c4["boards"].copy().view(pg.BOARD_DTYPE).reshape(-1)
     d4 = np.full(len(b4), 7, dtype=np.uint8)
-    pg.tt_clear()
-    st = pg.PgStats()
-    o_tt, s_tt = _timed(lambda: pg.perft_batch(b4, d4, use_tt=True, stats=st))
-    o_no, s_no = _timed(lambda: pg.perft_batch(b4, d4))
-    assert np.array_equal(o_tt, o_no)
-    tt["256_positions_depth7"] = {"leaves": int(o_tt.sum()), "tt_s": s_tt, "no_tt_s": s_no, "speedup": s_no / s_tt,
-                                  "tt_probes": st.tt_probes, "tt_hits": st.tt_hits, "tt_stores": st.tt_stores,
-                                  "tt_entry_gb_per_s": (st.tt_probes + st.tt_stores) * 16 / (st.device_ms / 1e3) / 1e9
-                                  if st.device_ms else None}
-    tt["note"] = ("TT: 781 seeded Zobrist keys, per-depth tables of 16-byte XOR-verified entries (32 GiB "
-                  "in total); every TT count equals the no-TT count")
+    tt["256_positions_depth7"] = tt_row(lambda **kw: pg.perft_batch(b4, d4, **kw), lambda r: int(r.sum()))
+    tt["note"] = ("128-bit Zobrist keys (two seeded 64-bit sets), per-depth tables of 32-byte entries with every "
+                  "key bit verified (32 GiB in total); every mode's count equals the no-TT count")
     out["transposition_table"] = tt
     return out
 
@@ -556,29 +566,40 @@ def run_ours(args):
             plain = {"value": tot / plain_s, "unit": "leaf nodes/s", "seconds": plain_s,
                      "calls": n, "timing": "host wall clock around the per-position calls"}
 
-        # roofline of the dominant kernel (k_leaf)
+        # roofline of the dominant kernel (k_leaf): integer-ALU issue, with the
+        # ALU warp instructions per leaf and the DRAM bytes per leaf-parent
+        # node of the ncu capture of this workload (every 16th position,
+        # profiles/k_leaf_batched_uneven_256.md) applied to the live leaf
+        # time of the timed steps; HBM as the secondary roofline
         peak, peak_kind, peaks = measured_peaks()
         per_launch_ms = leaf_ms / max(leaf_launches, 1)
         bytes_per_launch = leaf_nodes * LEAF_PARENT_BYTES / max(leaf_launches, 1)
         achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9 if per_launch_ms else 0.0
         traffic = None
         alu = None
-        tfile = os.path.join(ROOT, "profiles", "k_leaf_ks_position2_depth6_traffic.json")
+        tfile = os.path.join(ROOT, "profiles", "k_leaf_batched_uneven_256.json")
         if os.path.exists(tfile):
             with open(tfile) as f:
                 tj = json.load(f)
-            # DRAM bytes per leaf-parent node from the ncu capture of a smaller
-            # case of the same kernel, scaled to a launch by the nodes it reads
             traffic = tj["dram_bytes_per_leaf_parent"] * leaf_nodes / max(leaf_launches, 1)
-            # integer-ALU roofline: ALU warp instructions per leaf (ncu, same
-            # capture) x leaves per timed step / live k_leaf time
-            leaf_s = leaf_ms / 1e3 / args.steps
-            ach = tj["alu_warp_inst_per_leaf"] * leaves_per_step / leaf_s if leaf_s else 0.0
-            alu = {"bound": "alu", "kernel": "k_leaf", "achieved": ach / 1e9, "peak": tj["alu_peak_warp_inst_per_s"] / 1e9,
-                   "unit": "G warp-inst/s", "frac": ach / tj["alu_peak_warp_inst_per_s"],
+            sms = torch.cuda.get_device_properties(dev).multi_processor_count
+            mhz = float(peaks.get("sm_max_mhz") or clk.get("sm_max_mhz") or 2070.0)
+            alu_peak = tj["alu_peak_warp_inst_per_clk_per_sm"] * sms * mhz * 1e6
+            ach = tj["alu_warp_inst_per_leaf"] * leaves_per_step * args.steps / (leaf_ms / 1e3) if leaf_ms else 0.0
+            alu = {"bound": "alu", "kernel": "k_leaf", "achieved": ach / 1e9, "peak": alu_peak / 1e9,
+                   "unit": "G warp-inst/s", "frac": ach / alu_peak,
+                   "traffic": traffic,
                    "alu_warp_inst_per_leaf": tj["alu_warp_inst_per_leaf"],
-                   "peak_source": "2 ALU warp-instructions/clk/SM x 152 SMs x 2.07 GHz (nominal)",
+                   "achieved_def": "ALU warp-instructions per leaf (ncu, this workload) x leaves of the "
+                                   "timed steps / live k_leaf time (CUDA events)",
+                   "peak_source": "ncu sm__inst_executed_pipe_alu.avg.peak_sustained (%d/clk/SM) x %d SMs x "
+                                  "%.0f MHz (sm_max_mhz of MEASURED_PEAKS.json)"
+                                  % (tj["alu_peak_warp_inst_per_clk_per_sm"], sms, mhz),
                    "source": tj["source"]}
+        hbm = {"bound": "hbm", "kernel": "k_leaf", "achieved": achieved, "peak": peak, "unit": "GB/s",
+               "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+               "note": "algorithmic bytes: the leaf-parent boards read (53 B/node); leaves are counted, "
+                       "never stored"}
 
         workloads = None
         if not args.no_workloads:
@@ -587,7 +608,7 @@ def run_ours(args):
         served = None
         if not args.no_serve:
             rates = [float(x) for x in args.serve_rates.split(",")]
-            served = serve_leg(pg, rates, args.serve_seconds, rates[len(rates) // 2])
+            served = serve_leg(pg, rates, args.serve_seconds, 50.0 if 50.0 in rates else rates[len(rates) // 2])
 
         cpu = None
         if not args.no_cpu:
@@ -620,12 +641,8 @@ def run_ours(args):
             "autotune": pg.autotune(),
             "plain": plain,
             "batched_vs_plain": (value / plain["value"]) if plain else None,
-            "roofline": {"bound": "hbm", "kernel": "k_leaf", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "peak_source": peak_kind,
-                         "note": "integer-ALU-bound kernel: algorithmic bytes are the leaf-parent "
-                                 "boards read (53 B/node); see roofline_alu"},
-            "roofline_alu": alu,
+            "roofline": alu if alu is not None else hbm,
+            "roofline_hbm": hbm,
             "leaf_kernel": {"launches": leaf_launches, "ms_total": leaf_ms,
                             "ms_per_launch": per_launch_ms,
                             "share_of_timed": leaf_ms / (elapsed * 1e3)},
@@ -678,7 +695,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-workloads", action="store_true",
                     help="skip the other workloads (64 x depth 5, one position at depth 7, TT)")
-    ap.add_argument("--serve-rates", default="25,50,100", help="Poisson request rates (req/s)")
+    ap.add_argument("--serve-rates", default="25,50,75,100,150,200", help="Poisson request rates (req/s)")
     ap.add_argument("--serve-seconds", type=float, default=8.0)
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run N positions of the workload once and exit (small case for ncu)")

@@ -261,6 +261,17 @@ int pg_server_submit(const pg_board *pos, int depth, uint64_t *request_id);
 /* done = 1 once the count is final; latency_ms from submit to completion. */
 int pg_server_poll(uint64_t request_id, uint64_t *result, int *done, double *latency_ms);
 int pg_server_stop(void);
+/* Counters of the running server.  admissions_deferred counts the times the
+ * first waiting request did not fit the free frontier pool while others ran
+ * (it is then admitted first once a free block holds what it needs);
+ * pool_capacity / pool_peak are in positions (48 bytes each). */
+typedef struct pg_server_stats {
+    uint64_t submitted, completed, waves;
+    uint64_t admissions_deferred;
+    uint32_t max_active;         /* most requests in flight at once */
+    uint64_t pool_capacity, pool_peak;
+} pg_server_stats;
+int pg_server_get_stats(pg_server_stats *out);
 
 #ifdef __cplusplus
 }

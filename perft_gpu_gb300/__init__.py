@@ -132,6 +132,15 @@ class PgServerConfig(ctypes.Structure):
                 ("use_tt", ctypes.c_int), ("tt_bytes", ctypes.c_uint64)]
 
 
+class PgServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("waves", ctypes.c_uint64),
+                ("admissions_deferred", ctypes.c_uint64), ("max_active", ctypes.c_uint32),
+                ("pool_capacity", ctypes.c_uint64), ("pool_peak", ctypes.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _BP = ctypes.POINTER(HexaBitBoardPosition)
 _U16P = ctypes.POINTER(ctypes.c_uint16)
 _U32P = ctypes.POINTER(ctypes.c_uint32)
@@ -161,6 +170,7 @@ _SIGNATURES = {
     "pg_server_poll": [ctypes.c_uint64, _U64P, ctypes.POINTER(ctypes.c_int),
                        ctypes.POINTER(ctypes.c_double)],
     "pg_server_stop": [],
+    "pg_server_get_stats": [ctypes.POINTER(PgServerStats)],
     "pg_tt_clear": [],
     "pg_tt_save": [ctypes.c_char_p],
     "pg_tt_load": [ctypes.c_char_p],
@@ -443,6 +453,11 @@ class Server:
             if time.time() - t0 > timeout:
                 raise TimeoutError("request %d not done after %.0f s" % (rid, timeout))
             time.sleep(0.0005)
+
+    def stats(self) -> dict:
+        s = PgServerStats()
+        _check(load_library().pg_server_get_stats(ctypes.byref(s)))
+        return s.as_dict()
 
     def stop(self):
         _check(load_library().pg_server_stop())

@@ -641,7 +641,9 @@ static int perft_batch_device_locked(const Pos* d_pos, const unsigned char* d_de
 
 // The positions `plies` plies below root (all of them, in generateMoves
 // order level by level), written to out as boards; *n_out = their number.
-// Fails with PG_ERR_CAPACITY when they exceed cap or one level buffer.
+// Fails with PG_ERR_CAPACITY when they exceed cap or one level buffer; *n_out
+// is then the size of the level that did not fit (a lower bound of the
+// space the frontier needs).
 int expand_frontier(const Pos& root, int plies, Pos* out, u32 cap, u32* n_out)
 {
     Engine& E = engine();
@@ -673,6 +675,7 @@ int expand_frontier(const Pos& root, int plies, Pos* out, u32 cap, u32* n_out)
         total = E.host_scratch[0];
         if (total > cap || total > level_cap_max()) {
             set_error("frontier of %llu positions exceeds the capacity %u", (unsigned long long)total, cap);
+            *n_out = (u32)std::min<u64>(total, 0xFFFFFFFFull);  // a lower bound of the space needed
             return PG_ERR_CAPACITY;
         }
         if (total == 0) {

@@ -121,6 +121,7 @@ struct Request {
     int task_depth = 0;
     u64 acc_seen = 0;     // the request's counter after the last wave
     double per_task = 0;  // measured leaves per task (0 until a wave ran)
+    u64 need = 0;         // frontier boards known to be needed (after a deferred admission)
 };
 
 // first-fit allocator over the frontier pool (units: boards)
@@ -130,6 +131,12 @@ struct PoolAlloc {
     {
         free_.clear();
         if (cap) free_[0] = cap;
+    }
+    u64 largest() const
+    {
+        u64 m = 0;
+        for (const auto& kv : free_) m = std::max(m, kv.second);
+        return m;
     }
     bool take_largest(u64& off, u64& len)
     {
@@ -192,6 +199,9 @@ struct Server {
     u64* acc_host = nullptr;      // pinned
     // statistics
     u64 waves = 0;
+    u64 submitted = 0, completed = 0, deferred = 0;
+    u32 max_active = 0;
+    u64 pool_used = 0, pool_peak = 0;
 };
 
 Server* g_srv = nullptr;
@@ -214,6 +224,7 @@ double est_leaves(int d)
 
 void finish(Server& S, Request& r, int status, u64 result)
 {
+    S.completed++;
     r.status = status;
     r.result = result;
     r.t_done = now_s();
@@ -226,6 +237,16 @@ void admit(Server& S, std::unique_lock<std::mutex>& lk)
     while (!S.pending.empty() && !S.free_slots.empty()) {
         const u64 id = S.pending.front();
         Request& r = S.reqs[id];
+        if (r.need > S.pool_cap) {  // can never fit the pool
+            S.pending.pop_front();
+            set_error("request needs %llu frontier positions, over the pool of %llu", (unsigned long long)r.need,
+                      (unsigned long long)S.pool_cap);
+            finish(S, r, PG_ERR_CAPACITY, 0);
+            continue;
+        }
+        // a request that did not fit waits (first in line: no starvation)
+        // until a free block holds what it is known to need
+        if (r.need && S.alloc.largest() < r.need) return;
         u64 off = 0, len = 0;
         if (!S.alloc.take_largest(off, len)) return;  // pool full: wait for frees
         const int plies = r.depth > TASK_DEPTH ? r.depth - TASK_DEPTH : 0;
@@ -244,6 +265,8 @@ void admit(Server& S, std::unique_lock<std::mutex>& lk)
         }
         if (st == PG_ERR_CAPACITY && !S.active.empty()) {
             S.alloc.give(off, len);  // retry once running requests release memory
+            r.need = std::max<u64>(r.need, (u64)n + 1 > len ? (u64)n : len + 1);
+            S.deferred++;
             return;
         }
         S.pending.pop_front();
@@ -258,6 +281,8 @@ void admit(Server& S, std::unique_lock<std::mutex>& lk)
             continue;
         }
         S.alloc.give(off + n, len - n);
+        S.pool_used += n;
+        S.pool_peak = std::max(S.pool_peak, S.pool_used);
         r.slot = S.free_slots.back();
         S.free_slots.pop_back();
         r.pool_off = off;
@@ -266,6 +291,7 @@ void admit(Server& S, std::unique_lock<std::mutex>& lk)
         r.next = 0;
         r.task_depth = plies ? TASK_DEPTH : r.depth;
         S.active.push_back(id);
+        S.max_active = std::max<u32>(S.max_active, (u32)S.active.size());
     }
 }
 
@@ -373,6 +399,7 @@ int run_wave(Server& S, std::unique_lock<std::mutex>& lk)
         cudaMemsetAsync(S.acc + r.slot, 0, sizeof(u64), E.stream);
         S.free_slots.push_back(r.slot);
         S.alloc.give(r.pool_off, r.pool_len);
+        S.pool_used -= r.pool_len;
         r.slot = -1;
     }
     S.active.swap(still);
@@ -502,6 +529,7 @@ int pg_server_submit(const pg_board* pos, int depth, uint64_t* request_id)
     memcpy(&r.pos, pos, sizeof(Pos));
     r.depth = depth;
     r.t_submit = now_s();
+    S->submitted++;
     S->pending.push_back(id);
     *request_id = id;
     S->cv.notify_all();
@@ -531,6 +559,28 @@ int pg_server_poll(uint64_t request_id, uint64_t* result, int* done, double* lat
             return r.status;
         }
     }
+    return PG_OK;
+}
+
+int pg_server_get_stats(pg_server_stats* out)
+{
+    Server* S = g_srv;
+    if (!S) {
+        set_error("server not running");
+        return PG_ERR_NOT_INITIALIZED;
+    }
+    if (!out) {
+        set_error("null argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    out->submitted = S->submitted;
+    out->completed = S->completed;
+    out->waves = S->waves;
+    out->admissions_deferred = S->deferred;
+    out->max_active = S->max_active;
+    out->pool_capacity = S->pool_cap;
+    out->pool_peak = S->pool_peak;
     return PG_OK;
 }
 

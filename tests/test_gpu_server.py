@@ -102,3 +102,31 @@ def test_short_request_overtakes_running_deep_one(pg):
     assert n_deep == g2["perft7"]
     # completion times on the host clock: the short one first, by a margin
     assert t_short + lat_short / 1e3 < t_deep + lat_deep / 1e3 - 0.02, (lat_short, lat_deep)
+
+
+def test_hbm_admission_binds_and_no_request_starves(pg):
+    """A frontier pool that holds only one or two deep requests' frontiers at
+    once (3,200 positions; a depth-7 request keeps its positions two plies
+    below the root, about 1,000-2,500 of them, on the device): several deep requests
+    submitted together are admitted as space frees up, first in line first.
+    Every count equals the batch engine's count of the same request, every
+    request completes, and the counters show that memory, not slots, bounded
+    admission."""
+    g2 = golden_json("config2.json")
+    deep = pg.HexaBitBoardPosition(*words_of_hex(g2["board"]))
+    boards, _ = pg.random_playouts(57, 8, 10, 30, 32, with_depths=True)
+    reqs = [(pg.board_of(b), 7) for b in boards] + [(deep, 7)]
+    want = pg.perft_batch(pg.boards_array([b for b, _ in reqs]), [d for _, d in reqs])
+    assert int(want[-1]) == g2["perft7"]
+    srv = pg.Server(hbm_budget_bytes=3200 * 48, max_inflight=64)
+    try:
+        ids = [srv.submit(b, d) for b, d in reqs]
+        got = [srv.wait(r, timeout=300)[0] for r in ids]
+        st = srv.stats()
+    finally:
+        srv.stop()
+    assert got == [int(x) for x in want]
+    assert st["completed"] == st["submitted"] == len(reqs)
+    assert st["admissions_deferred"] > 0
+    assert st["max_active"] >= 2
+    assert 0 < st["pool_peak"] <= st["pool_capacity"] == 3200
