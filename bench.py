@@ -264,7 +264,8 @@ def serve_leg(pg, rates, seconds, plain_rate):
     boards, depths, rng = serve_requests(pg, max_n)
     out = {"requests": "seeded playout positions (0-60 plies), depth lognormal(median 4, sigma 0.25) "
                        "clipped to 3..8; Poisson arrivals", "rates": [],
-           "stable_def": "completions per second >= 95% of the offered rate over the run"}
+           "stable_def": "offered load (leaves of the requests / arrival window) at most 90% of the "
+                         "saturated throughput (served leaves/s at the highest swept rate)"}
     check_n = 0
     for rate in rates:
         arrivals = np.cumsum(rng.exponential(1.0 / rate, max_n))
@@ -288,7 +289,12 @@ def serve_leg(pg, rates, seconds, plain_rate):
         check_n += n
         out["rates"].append({"rate_req_s": rate, "requests": n, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
                              "max_ms": max(lat) if lat else None, "leaves_per_s": leaves / wall,
-                             "completed_per_s": n / wall, "stable": n / wall >= 0.95 * rate})
+                             "offered_leaves_per_s": leaves / float(arrivals[n - 1]) if n else 0.0,
+                             "completed_per_s": n / wall})
+    saturated = max(r["leaves_per_s"] for r in out["rates"])
+    for r in out["rates"]:
+        r["utilization"] = r["offered_leaves_per_s"] / saturated
+        r["stable"] = r["utilization"] <= 0.9
     stable = [r for r in out["rates"] if r["stable"]]
     if stable:
         top = max(stable, key=lambda r: r["rate_req_s"])
