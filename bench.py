@@ -539,6 +539,35 @@ def run_ours(args):
     graph_value = leaves_per_step * args.steps * world / graph_el
     assert int(d_out.cpu().numpy().view(np.uint64).sum()) == leaves_per_step
 
+    # the same steps as one persistent cooperative launch per step (levels
+    # and chunks walked on the device), and that launch replayed from a graph
+    def step_persist(graph):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        pg.perft_batch_device(d_boards.data_ptr(), d_depths.data_ptr(), n, d_out.data_ptr(), persistent=True,
+                              graph=graph)
+
+    persist = {}
+    psteps = min(args.steps, 5)
+    for name, graph in (("launch", False), ("graph", True)):
+        step_persist(graph)
+        assert int(d_out.cpu().numpy().view(np.uint64).sum()) == leaves_per_step
+        barrier(dist)
+        torch.cuda.synchronize()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(psteps):
+            step_persist(graph)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        el = max_over_ranks(dist, p0.elapsed_time(p1) / 1e3)
+        assert int(d_out.cpu().numpy().view(np.uint64).sum()) == leaves_per_step
+        persist[name] = {"value": leaves_per_step * psteps * world / el, "unit": "leaf nodes/s",
+                         "ms_per_step": 1e3 * el / psteps, "steps": psteps}
+    persist["note"] = ("one cooperative persistent launch per step (Kogge-Stone, 128-thread CTAs, two-ply leaf); "
+                       "'graph': that launch replayed from a captured graph (valid for any contents)")
+
     # end to end through the public API with host buffers
     pin_b = torch.from_numpy(boards.view(np.uint8).copy()).pin_memory()
     pin_d = torch.from_numpy(depths.copy()).pin_memory()
@@ -641,6 +670,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "leaf nodes/s",
                     "h2d_bytes_per_step": n * 48 + n, "d2h_bytes_per_step": n * 8},
             "gpu_launches": launches,
+            "persistent": persist,
             "graph_replay": {"value": graph_value, "unit": "leaf nodes/s",
                              "ms_per_step": 1e3 * graph_el / args.steps,
                              "note": "same steps replayed from one captured CUDA graph per step"},

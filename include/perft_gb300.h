@@ -99,6 +99,10 @@ typedef struct pg_opts {
     uint64_t tt_bytes;           /* total TT bytes across depths; 0 = from budget */
     int graph;                   /* replay the call's launch sequence from a captured CUDA graph */
     pg_stats *stats;             /* optional out */
+    int persistent;              /* the whole batch as one persistent cooperative launch that walks
+                                    the levels and chunks on the device (Kogge-Stone sliders, 128-thread
+                                    CTAs, two-ply leaf; no TT): the reference's device-side driver,
+                                    perft_bb.h:1143-1220, without dynamic parallelism */
 } pg_opts;
 
 /* ---- engine ---- */
@@ -253,6 +257,7 @@ typedef struct pg_server_config {
     int use_tt;                  /* pg_tt_mode of the waves; with PG_TT_ON the tables persist
                                     across requests (launcher.h:699-790 keeps its table across runs) */
     uint64_t tt_bytes;           /* TT size when use_tt; 0 = from the engine budget (as pg_opts) */
+    int persistent;              /* run each wave (without TT) as one persistent launch (pg_opts.persistent) */
 } pg_server_config;
 
 int pg_server_start(const pg_server_config *cfg);

@@ -109,7 +109,7 @@ class PgOpts(ctypes.Structure):
     _fields_ = [("slider", ctypes.c_int), ("block_size", ctypes.c_int),
                 ("leaf_plies", ctypes.c_int), ("use_tt", ctypes.c_int),
                 ("tt_bytes", ctypes.c_uint64), ("graph", ctypes.c_int),
-                ("stats", ctypes.POINTER(PgStats))]
+                ("stats", ctypes.POINTER(PgStats)), ("persistent", ctypes.c_int)]
 
 
 class PgTuning(ctypes.Structure):
@@ -129,7 +129,7 @@ class PgTuning(ctypes.Structure):
 class PgServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
                 ("slider", ctypes.c_int), ("max_wave_nodes", ctypes.c_uint32),
-                ("use_tt", ctypes.c_int), ("tt_bytes", ctypes.c_uint64)]
+                ("use_tt", ctypes.c_int), ("tt_bytes", ctypes.c_uint64), ("persistent", ctypes.c_int)]
 
 
 class PgServerStats(ctypes.Structure):
@@ -223,7 +223,8 @@ def _tt_mode(use_tt) -> int:
     return int(use_tt)
 
 
-def _opts(slider=None, block_size=0, use_tt=False, tt_bytes=0, graph=False, stats=None, leaf_plies=0):
+def _opts(slider=None, block_size=0, use_tt=False, tt_bytes=0, graph=False, stats=None, leaf_plies=0,
+          persistent=False):
     o = PgOpts()
     o.slider = SLIDERS[slider] if isinstance(slider, str) else (slider or 0)
     o.block_size = block_size
@@ -231,6 +232,7 @@ def _opts(slider=None, block_size=0, use_tt=False, tt_bytes=0, graph=False, stat
     o.use_tt = _tt_mode(use_tt)
     o.tt_bytes = tt_bytes
     o.graph = 1 if graph else 0
+    o.persistent = 1 if persistent else 0
     o.stats = ctypes.pointer(stats) if stats is not None else None
     return o
 
@@ -425,10 +427,11 @@ class Server:
     """Continuous-batching perft server (pg_server_*)."""
 
     def __init__(self, hbm_budget_bytes: int = 0, max_inflight: int = 0, slider: int | str = 0,
-                 max_wave_nodes: int = 0, use_tt: bool | int | str = False, tt_bytes: int = 0):
+                 max_wave_nodes: int = 0, use_tt: bool | int | str = False, tt_bytes: int = 0,
+                 persistent: bool = False):
         cfg = PgServerConfig(hbm_budget_bytes, max_inflight,
                              SLIDERS[slider] if isinstance(slider, str) else slider, max_wave_nodes,
-                             _tt_mode(use_tt), tt_bytes)
+                             _tt_mode(use_tt), tt_bytes, 1 if persistent else 0)
         _check(load_library().pg_server_start(ctypes.byref(cfg)))
 
     def submit(self, pos: HexaBitBoardPosition, depth: int) -> int:

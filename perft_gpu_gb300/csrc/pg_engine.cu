@@ -491,6 +491,10 @@ static int end_call(const pg_opts* o)
     PG_CUDA(cudaMemcpyAsync(E.host_scratch, E.err, sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
     PG_CUDA(cudaStreamSynchronize(E.stream));
     errv = (u32)E.host_scratch[0];
+    if (errv & (ERR_PLAN_OVERFLOW | ERR_LEVEL_CAP)) {
+        set_error("device error flags 0x%x: the work exceeded a fixed-size plan or level", errv);
+        return PG_ERR_CAPACITY;
+    }
     if (errv & 0xFFFFFFFFu) {
         set_error("device error flags 0x%x", errv);
         return PG_ERR_DEVICE_TIMEOUT;
@@ -548,6 +552,73 @@ int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_gro
     return PG_OK;
 }
 
+int perft_core_persistent(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc,
+                          bool zero_acc, int maxd);
+static int prepare_persist(u32 n, int maxd, PersistArgs& A);
+static int device_max_depth(const unsigned char* d_depths, u32 n, int* maxd);
+
+// The persistent launch replayed from a graph: its chunk plans are made on
+// the device, so a captured graph (a few memsets and the one cooperative
+// launch) stays valid for any contents of the same buffers, size and largest
+// depth (the level buffers are prepared for it); only the largest depth is
+// read back per call.
+static int perft_batch_graph_persistent(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out)
+{
+    Engine& E = engine();
+    int maxd = 0;
+    PG_TRY(device_max_depth(d_depths, n, &maxd));
+    if (maxd > 15) {
+        set_error("depth %d out of range 0..15", maxd);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    GraphCache& g = E.graph;
+    const bool hit = g.exec && g.persistent && g.alloc_gen == E.alloc_gen && g.pos == d_pos && g.dep == d_depths &&
+                     g.out == d_out && g.n == n && g.maxd == maxd;
+    if (!hit) {
+        PersistArgs A;
+        PG_TRY(prepare_persist(n, maxd, A));  // every allocation before the capture
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = GraphCache{};
+        cudaGraph_t graph = nullptr;
+        PG_CUDA(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
+        E.plan_mode = PLAN_REPLAY;
+        const int rc = perft_core_persistent(d_pos, d_depths, nullptr, n, d_out, true, maxd);
+        E.plan_mode = PLAN_NONE;
+        const cudaError_t ce = cudaStreamEndCapture(E.stream, &graph);
+        if (rc != PG_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        PG_CUDA(ce);
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        PG_CUDA(ie);
+        g.exec = exec;
+        g.persistent = true;
+        g.maxd = maxd;
+        g.pos = d_pos;
+        g.dep = d_depths;
+        g.out = d_out;
+        g.n = n;
+        g.launches = 1;
+        g.alloc_gen = E.alloc_gen;
+        E.st.graph_captures = 1;
+    } else {
+        E.st.graph_replays = 1;
+    }
+    cudaEventRecord(E.ev0, E.stream);
+    PG_CUDA(cudaGraphLaunch(g.exec, E.stream));
+    cudaEventRecord(E.ev1, E.stream);
+    PG_CUDA(cudaEventSynchronize(E.ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+    E.st.device_ms = ms;
+    E.st.leaf_kernel_ms = ms;
+    E.st.launches = 1;
+    return PG_OK;
+}
+
 // Batch perft replayed from a captured CUDA graph.  The first call on a set
 // of inputs runs normally while recording its data-dependent launch plan
 // (root partition, chunk boundaries), then captures the same launch sequence
@@ -569,7 +640,7 @@ static int perft_batch_graph_locked(const Pos* d_pos, const unsigned char* d_dep
     GraphCache& g = E.graph;
     // a graph names the level, scan and staging buffers of its capture: any
     // reallocation since (alloc_gen) makes it stale, never replayed
-    const bool hit = g.exec && g.alloc_gen == E.alloc_gen && g.pos == d_pos && g.dep == d_depths && g.out == d_out &&
+    const bool hit = g.exec && !g.persistent && g.alloc_gen == E.alloc_gen && g.pos == d_pos && g.dep == d_depths && g.out == d_out &&
                      g.n == n && g.sum == sum && g.slider == v.slider && g.T == v.T &&
                      g.leaf_plies == v.leaf_plies && g.per_depth == v.per_depth;
     if (hit) {
@@ -632,10 +703,120 @@ static int perft_batch_graph_locked(const Pos* d_pos, const unsigned char* d_dep
     return PG_OK;
 }
 
-// batch perft with device inputs; d_out must not alias the inputs
-static int perft_batch_device_locked(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out,
-                                     const pg_opts* o)
+// The buffers of a persistent launch of roots up to depth maxd: every level
+// down to the leaf-parent level (maxd - 2, the two-ply leaf) is prepared
+// before the launch.  The leaf-parent level gets up to the largest level
+// (level_cap_max), each level above it a 16th of the one below (a chunk of
+// it still fills the level below about twice), no level less than 65,536
+// nodes or more than it can hold (n x 40^L): chunks keep the launch correct
+// at any capacity.
+static int prepare_persist(u32 n, int maxd, PersistArgs& A)
 {
+    Engine& E = engine();
+    memset(&A, 0, sizeof(A));
+    const int deepest = std::min(std::max(maxd - 2, 0), MAX_LEVELS - 1);
+    const u64 capmax = level_cap_max();
+    u64 status_words = 0;
+    for (int L = 0; L <= deepest; L++) {
+        u64 cap = n;
+        if (L > 0) {
+            double est = (double)n;
+            for (int k = 0; k < L; k++) est *= 40.0;
+            const u64 bound = capmax >> std::min(60, 4 * (deepest - L));
+            cap = (u64)std::min(est, (double)bound);
+            cap = std::max<u64>(cap, 1u << 16);
+        }
+        PG_TRY(ensure_level(L, cap));
+        const LevelBuf& lb = E.lv[L];
+        A.lv[L] = lb.v;
+        A.cnt[L] = lb.cnt;
+        A.offs[L] = lb.offs;
+        A.cap[L] = lb.cap;
+        status_words = std::max<u64>(status_words, lb.cap / PERSIST_SCAN_TILE_NODES + 2);
+    }
+    if (status_words > E.scan_status_cap) {
+        E.alloc_gen++;
+        PG_CUDA(cudaStreamSynchronize(E.stream));
+        if (E.scan_status) cudaFree(E.scan_status);
+        E.scan_status = nullptr;
+        E.scan_status_cap = 0;
+        PG_CUDA(cudaMalloc(&E.scan_status, status_words * sizeof(u64)));
+        E.scan_status_cap = status_words;
+    }
+    if (!E.persist_plan) PG_CUDA(cudaMalloc(&E.persist_plan, MAX_LEVELS * sizeof(PlanOut)));
+    if (!E.persist_ctl) PG_CUDA(cudaMalloc(&E.persist_ctl, sizeof(PersistCtl)));
+    A.plan = E.persist_plan;
+    A.status = E.scan_status;
+    A.status_cap = E.scan_status_cap;
+    A.tickets = E.tickets;
+    A.max_tickets = MAX_TICKETS - 8;
+    A.ctl = E.persist_ctl;
+    A.err = E.err;
+    return PG_OK;
+}
+
+// the largest depth of a device batch (one readback)
+static int device_max_depth(const unsigned char* d_depths, u32 n, int* maxd)
+{
+    Engine& E = engine();
+    u32* d = (u32*)E.aux;
+    PG_CUDA(cudaMemsetAsync(d, 0, sizeof(u32), E.stream));
+    k_max_depth<<<std::max<u32>(1, std::min<u32>((n + 255) / 256, 1024)), 256, 0, E.stream>>>(d_depths, n, d);
+    PG_CUDA(cudaGetLastError());
+    u32* h = (u32*)(E.host_scratch + 160);
+    PG_CUDA(cudaMemcpyAsync(h, d, sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+    PG_CUDA(cudaStreamSynchronize(E.stream));
+    *maxd = (int)*h;
+    return PG_OK;
+}
+
+// perft of n roots in one persistent launch; each root's count is added to
+// acc[group] (group = groups[i], or i when groups is null), acc zeroed first
+// when zero_acc; maxd = the largest depth of the roots
+int perft_core_persistent(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc,
+                          bool zero_acc, int maxd)
+{
+    Engine& E = engine();
+    if (maxd > 15) {
+        set_error("depth %d out of range 0..15", maxd);
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    PersistArgs A;
+    PG_TRY(prepare_persist(n, maxd, A));
+    A.pos = d_pos;
+    A.depths = d_depths;
+    A.groups = d_groups;
+    A.n = n;
+    A.acc = acc;
+    if (zero_acc) PG_CUDA(cudaMemsetAsync(acc, 0, (u64)n * sizeof(u64), E.stream));
+    PG_CUDA(cudaMemsetAsync(E.persist_ctl, 0, sizeof(PersistCtl), E.stream));
+    PG_CUDA(cudaMemsetAsync(&E.persist_ctl->part[2], 0xFF, sizeof(u32), E.stream));
+    PG_CUDA(cudaMemsetAsync(E.tickets, 0, MAX_TICKETS * sizeof(u32), E.stream));
+    const bool capturing = E.plan_mode == PLAN_REPLAY;
+    if (!capturing) cudaEventRecord(E.ev0, E.stream);
+    int grid = 0;
+    PG_CUDA(persist_launch(A, E.stream, E.num_sms, &grid));
+    E.st.launches++;
+    if (!capturing) {
+        cudaEventRecord(E.ev1, E.stream);
+        PG_CUDA(cudaEventSynchronize(E.ev1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+        E.st.device_ms = ms;
+        E.st.leaf_kernel_ms = ms;  // one kernel: its leaf phases are not timed apart
+    }
+    return PG_OK;
+}
+
+// batch perft with device inputs; d_out must not alias the inputs; maxd the
+// batch's largest depth when the caller knows it (else -1)
+static int perft_batch_device_locked(const Pos* d_pos, const unsigned char* d_depths, u32 n, u64* d_out,
+                                     const pg_opts* o, int maxd = -1)
+{
+    if (o && o->persistent) {
+        if (maxd < 0) PG_TRY(device_max_depth(d_depths, n, &maxd));
+        return perft_core_persistent(d_pos, d_depths, nullptr, n, d_out, true, maxd);
+    }
     return perft_core(d_pos, d_depths, nullptr, n, d_out, true, pick_variant(o));
 }
 
@@ -890,6 +1071,10 @@ static void release_engine(Engine& E)
     if (E.plan_host) cudaFreeHost(E.plan_host);
     if (E.host_scratch) cudaFreeHost(E.host_scratch);
     if (E.aux) cudaFree(E.aux);
+    if (E.persist_plan) cudaFree(E.persist_plan);
+    if (E.persist_ctl) cudaFree(E.persist_ctl);
+    E.persist_plan = nullptr;
+    E.persist_ctl = nullptr;
     if (E.graph.exec) cudaGraphExecDestroy(E.graph.exec);
     E.graph = GraphCache{};
     for (cudaEvent_t* ev : {&E.ev0, &E.ev1})
@@ -1197,6 +1382,8 @@ int pg_perft_batch_device(const pg_board* d_pos, const uint8_t* d_depths, uint32
     PG_TRY(begin_call(opts));
     if (opts && opts->use_tt) {
         PG_TRY(tt_perft_batch_device((const Pos*)d_pos, d_depths, n, (u64*)d_out, opts));
+    } else if (opts && opts->graph && opts->persistent) {
+        PG_TRY(perft_batch_graph_persistent((const Pos*)d_pos, d_depths, n, (u64*)d_out));
     } else if (opts && opts->graph) {
         PG_TRY(perft_batch_graph_locked((const Pos*)d_pos, d_depths, n, (u64*)d_out, opts));
     } else {
@@ -1228,10 +1415,14 @@ int pg_perft_batch(const pg_board* pos, const uint8_t* depths, uint32_t n, uint6
     PG_CUDA(cudaMemcpyAsync(d_dep, depths, n, cudaMemcpyHostToDevice, E.stream));
     if (opts && opts->use_tt) {
         PG_TRY(tt_perft_batch_device(d_pos, d_dep, n, d_out, opts));
+    } else if (opts && opts->graph && opts->persistent) {
+        PG_TRY(perft_batch_graph_persistent(d_pos, d_dep, n, d_out));
     } else if (opts && opts->graph) {
         PG_TRY(perft_batch_graph_locked(d_pos, d_dep, n, d_out, opts));
     } else {
-        PG_TRY(perft_batch_device_locked(d_pos, d_dep, n, d_out, opts));
+        int maxd = 0;
+        for (u32 i = 0; i < n; i++) maxd = std::max<int>(maxd, depths[i]);
+        PG_TRY(perft_batch_device_locked(d_pos, d_dep, n, d_out, opts, maxd));
     }
     PG_CUDA(cudaMemcpyAsync(out, d_out, ob, cudaMemcpyDeviceToHost, E.stream));
     PG_TRY(end_call(nullptr));

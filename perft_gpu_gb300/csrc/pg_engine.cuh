@@ -24,6 +24,7 @@ enum : u32 {
     ERR_QUEUE_MISMATCH = 1u << 3,
     ERR_GRID_BARRIER_TIMEOUT = 1u << 4,
     ERR_TT_GUARD = 1u << 5,
+    ERR_LEVEL_CAP = 1u << 6,  // a persistent launch reached a level the host did not prepare
 };
 
 // one frontier level in HBM: boards as three 16-byte planes (struct of
@@ -54,6 +55,41 @@ struct PlanOut {
 
 enum PlanMode { PLAN_NONE = 0, PLAN_RECORD = 1, PLAN_REPLAY = 2 };
 
+// control words of one persistent launch (pg_persist.cuh; device memory,
+// zeroed by the host before the launch, part[2] = 0xFFFFFFFF): grid barrier
+// arrival count and generation, abort flag, root partition counters (white,
+// black, min depth, max depth)
+struct PersistCtl {
+    u32 bar_count, bar_gen, abort, pad;
+    u32 part[4];
+};
+
+// arguments of one persistent launch: the roots, the level buffers the host
+// prepared (cap 0 = not prepared), per-level chunk plans, scan status words,
+// phase tickets (zeroed), control words, error bits
+struct PersistArgs {
+    const Pos* pos;
+    const unsigned char* depths;
+    const u32* groups;  // group id per root (null: the root's index)
+    u32 n;
+    u64* acc;  // per-group counts (added to)
+    LevelView lv[MAX_LEVELS];
+    u32* cnt[MAX_LEVELS];
+    u64* offs[MAX_LEVELS];
+    u64 cap[MAX_LEVELS];
+    PlanOut* plan;  // MAX_LEVELS plans
+    u64* status;
+    u64 status_cap;
+    u32* tickets;
+    u32 max_tickets;
+    PersistCtl* ctl;
+    u32* err;
+};
+// the persistent launch (Kogge-Stone translation unit); *grid = CTAs launched
+cudaError_t persist_launch(const PersistArgs& a, cudaStream_t st, int num_sms, int* grid);
+constexpr int PERSIST_CTA = 128;  // threads per CTA of the persistent launch
+constexpr u32 PERSIST_SCAN_TILE_NODES = 1024;  // counts per scan tile of the persistent launch
+
 // one captured batch (see perft_batch_graph_locked)
 struct GraphCache {
     cudaGraphExec_t exec = nullptr;
@@ -66,6 +102,8 @@ struct GraphCache {
     bool per_depth = false;
     u64 launches = 0;
     u64 alloc_gen = 0;  // Engine::alloc_gen when captured
+    bool persistent = false;  // one persistent launch: valid for any contents of the same size and largest depth
+    int maxd = 0;
 };
 
 struct Engine {
@@ -98,6 +136,8 @@ struct Engine {
     u64 stage_cap = 0;
     u64* host_scratch = nullptr;   // pinned small scratch
     u64* aux = nullptr;            // small device scratch (input checksum)
+    PlanOut* persist_plan = nullptr;  // MAX_LEVELS chunk plans of a persistent launch
+    PersistCtl* persist_ctl = nullptr;
     // launch-plan recording for graph capture
     int plan_mode = PLAN_NONE;
     std::vector<std::vector<u32>> rec_bnd;
@@ -145,5 +185,7 @@ int ensure_stage(u64 bytes);
 int perft_core(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc, bool zero_acc,
                const Variant& v);
 int expand_frontier(const Pos& root, int plies, Pos* out, u32 cap, u32* n_out);
+int perft_core_persistent(const Pos* d_pos, const unsigned char* d_depths, const u32* d_groups, u32 n, u64* acc,
+                          bool zero_acc, int maxd);
 
 }  // namespace pg

@@ -228,14 +228,25 @@ __global__ void k_playouts(Pos start, u64 seed, u32 n, int min_plies, int max_pl
 // engine kernels
 // ---------------------------------------------------------------------------
 
+// The bodies of the level kernels are device functions so that the
+// persistent driver (pg_persist.cuh) runs the same code as the per-level
+// launches; the kernels below are thin wrappers.  The bodies take no
+// __restrict__ on data another phase of a persistent launch writes.
+
 template <int S, class SL>
-__global__ void k_count_level(LevelView lv, u32 start, u32 n, u32* __restrict__ cnt, u32 min_rem)
+__device__ __forceinline__ void count_level_body(const LevelView& lv, u32 start, u32 n, u32* cnt, u32 min_rem)
 {
-    stage_tables<SL>();
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const u32 rem = lv.rem[start + i];
         cnt[i] = (rem >= min_rem && rem < REM_DEAD) ? count_moves<S, SL>(load_board(lv, start + i)) : 0u;
     }
+}
+
+template <int S, class SL>
+__global__ void k_count_level(LevelView lv, u32 start, u32 n, u32* __restrict__ cnt, u32 min_rem)
+{
+    stage_tables<SL>();
+    count_level_body<S, SL>(lv, start, n, cnt, min_rem);
 }
 
 template <class SL, int T, int QCAP> struct BlockSmem {
@@ -258,11 +269,9 @@ template <int T> constexpr int min_blocks() { return (PG_LEAF_MIN_WARPS * 32 + T
 // queued children, one at a time.  A CTA's children normally fit one queue
 // window; when they do not, the later windows generate again.
 template <int S, class SL, int T, int QCAP>
-__global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
-                                                            u32 max_rem)
+__device__ __forceinline__ void leaf_body(const LevelView& lv, u32 start, u32 n, u64* acc, u32* ticket, u32 max_rem,
+                                          unsigned char* pg_dyn_smem)
 {
-    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
-    stage_tables<SL>();
     using L = BlockSmem<SL, T, QCAP>;
     Pos* sb = reinterpret_cast<Pos*>(pg_dyn_smem + L::tables);
     u32* q = reinterpret_cast<u32*>(pg_dyn_smem + L::tables + L::boards);
@@ -346,16 +355,24 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
     ga.flush_warp(acc);
 }
 
+template <int S, class SL, int T, int QCAP>
+__global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
+                                                            u32 max_rem)
+{
+    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
+    stage_tables<SL>();
+    leaf_body<S, SL, T, QCAP>(lv, start, n, acc, ticket, max_rem, pg_dyn_smem);
+}
+
 // children of the nodes [a, b) of a level into the next level; offs is the
 // exclusive scan of the children counts, child slots start at offs[a]
 // parent_out (transposition-table mode): each child's group becomes its own
 // slot and its parent's slot is written to parent_out
 template <int S, class SL, int T, int QCAP>
-__global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32 start, u32 a, u32 b, const u64* __restrict__ offs,
-                                              LevelView out, u32* ticket, u32* __restrict__ parent_out = nullptr)
+__device__ __forceinline__ void expand_body(const LevelView& in, u32 start, u32 a, u32 b, const u64* offs,
+                                            const LevelView& out, u32* ticket, u32* parent_out,
+                                            unsigned char* pg_dyn_smem)
 {
-    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
-    stage_tables<SL>();
     using L = BlockSmem<SL, T, QCAP>;
     Pos* sb = reinterpret_cast<Pos*>(pg_dyn_smem + L::tables);
     u32* q = reinterpret_cast<u32*>(pg_dyn_smem + L::tables + L::boards);
@@ -412,6 +429,15 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32
         }
         __syncthreads();
     }
+}
+
+template <int S, class SL, int T, int QCAP>
+__global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32 start, u32 a, u32 b, const u64* __restrict__ offs,
+                                              LevelView out, u32* ticket, u32* __restrict__ parent_out = nullptr)
+{
+    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
+    stage_tables<SL>();
+    expand_body<S, SL, T, QCAP>(in, start, a, b, offs, out, ticket, parent_out, pg_dyn_smem);
 }
 
 }  // namespace pg

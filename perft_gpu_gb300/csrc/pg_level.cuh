@@ -156,6 +156,15 @@ static __global__ void k_plan(const u64* __restrict__ offs, u32 n, u64 cap, Plan
     plan->total = offs[n];
 }
 
+// largest depth of a batch (out zeroed by the caller)
+static __global__ void k_max_depth(const unsigned char* __restrict__ dep, u32 n, u32* out)
+{
+    u32 m = 0;
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = max(m, (u32)dep[i]);
+    m = __reduce_max_sync(0xFFFFFFFFu, m);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
 // order-sensitive 64-bit checksum of a batch (boards and depths)
 static __global__ void k_checksum(const Pos* __restrict__ pos, const unsigned char* __restrict__ dep, u32 n, u64* out)
 {

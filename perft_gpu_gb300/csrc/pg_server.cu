@@ -181,6 +181,7 @@ struct Server {
     u32 max_inflight = 4096;
     int slider = 0;
     int use_tt = PG_TT_OFF;  // pg_tt_mode of the waves
+    bool persistent = false;  // waves as one persistent launch
     u64 tt_bytes = 0;
     double wave_leaves = 4e9;  // fixed wave budget (max_wave_nodes) or the first wave's
     bool timed_waves = true;   // size waves from the measured rate
@@ -360,6 +361,10 @@ int run_wave(Server& S, std::unique_lock<std::mutex>& lk)
                                                                                        total, S.acc);
             if (cudaGetLastError() != cudaSuccess) st = PG_ERR_CUDA;
         }
+    } else if (S.persistent) {
+        int maxd = 0;
+        for (const Segment& sg : segs) maxd = std::max<int>(maxd, (int)sg.depth);
+        st = perft_core_persistent(S.wave_pos, S.wave_dep, S.wave_grp, total, S.acc, false, maxd);
     } else {
         st = perft_core(S.wave_pos, S.wave_dep, S.wave_grp, total, S.acc, false, pick_variant(&o));
     }
@@ -470,6 +475,7 @@ int pg_server_start(const pg_server_config* cfg)
         return PG_ERR_INVALID_ARGUMENT;
     }
     S->tt_bytes = cfg ? cfg->tt_bytes : 0;
+    S->persistent = cfg && cfg->persistent;
     if (cfg && cfg->max_wave_nodes) {
         S->wave_leaves = (double)cfg->max_wave_nodes * est_leaves(TASK_DEPTH);
         S->timed_waves = false;

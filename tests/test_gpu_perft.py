@@ -186,3 +186,82 @@ def test_graph_recaptured_after_buffers_are_reallocated(pg):
     assert pg.perft_batch(big, big_d, slider="ks").sum() > 0
     assert graph_call() == (1, 0)
     assert graph_call() == (0, 1)
+
+
+def test_persistent_launch_matches_golden(pg):
+    """The whole batch as one persistent cooperative launch (levels, chunks
+    and phases walked on the device): the reference's golden counts, one
+    kernel launch per call."""
+    import torch
+    g = golden_npz("config3.npz")
+    idx = np.arange(0, 4096, 7)
+    boards = g["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    st = pg.PgStats()
+    out = pg.perft_batch(boards, g["depths"][idx], persistent=True, stats=st)
+    assert np.array_equal(out, g["totals"][idx])
+    assert st.launches == 1
+    # every golden FEN depth in one mixed batch (depths 0..2 take only the leaf phase)
+    bs, ds, want = [], [], []
+    for f in golden_json("fens.json"):
+        b = pg.board_from_fen(f["fen"])
+        for d, v in f["perft"].items():
+            if int(d) <= 5:
+                bs.append(b)
+                ds.append(int(d))
+                want.append(v)
+    assert [int(x) for x in pg.perft_batch(pg.boards_array(bs), ds, persistent=True)] == want
+    # device pointers (the largest depth is read back once)
+    d_b = torch.from_numpy(g["boards"][idx].copy().view(np.uint8)).cuda()
+    d_d = torch.from_numpy(g["depths"][idx].copy()).cuda()
+    d_o = torch.zeros(len(idx), dtype=torch.int64, device="cuda")
+    pg.perft_batch_device(d_b.data_ptr(), d_d.data_ptr(), len(idx), d_o.data_ptr(), persistent=True)
+    assert np.array_equal(d_o.cpu().numpy().view(np.uint64), g["totals"][idx])
+
+
+def test_persistent_launch_deep_position(pg):
+    g = golden_json("config2.json")
+    b = pg.HexaBitBoardPosition(*words_of_hex(g["board"]))
+    assert pg.perft(b, 7, persistent=True) == g["perft7"]
+
+
+def test_persistent_launch_chunked_small_budget(pg):
+    """A 64 MB budget gives the persistent launch small levels: the device
+    splits levels into many chunks and walks them depth first."""
+    item = golden_json("fens.json")[1]
+    pg.shutdown()
+    pg.init(hbm_budget_bytes=64 << 20)
+    try:
+        b = pg.board_from_fen(item["fen"])
+        assert pg.perft(b, 5, persistent=True) == item["perft"]["5"]
+        g = golden_npz("config4_d5.npz")
+        boards = g["boards"][:64].copy().view(pg.BOARD_DTYPE).reshape(-1)
+        assert np.array_equal(pg.perft_batch(boards, [5] * 64, persistent=True), g["totals"][:64])
+    finally:
+        pg.shutdown()
+        pg.init()
+
+
+def test_persistent_graph_replays_any_contents(pg):
+    """The persistent launch captured in a graph plans its chunks on the
+    device: new contents in the same buffers (same size and largest depth)
+    replay the same graph and give their own golden counts."""
+    import torch
+    g = golden_npz("config3.npz")
+    a = np.arange(0, 4096, 13)
+    b = np.arange(5, 4096, 13)[:len(a)]
+    sel = [a, b]
+    assert g["depths"][a].max() == g["depths"][b].max()
+    d_b = torch.from_numpy(g["boards"][a].copy().view(np.uint8)).cuda()
+    d_d = torch.from_numpy(g["depths"][a].copy()).cuda()
+    d_o = torch.zeros(len(a), dtype=torch.int64, device="cuda")
+    seen = []
+    for k in range(4):
+        idx = sel[k // 2]
+        d_b.copy_(torch.from_numpy(g["boards"][idx].copy().view(np.uint8)))
+        d_d.copy_(torch.from_numpy(g["depths"][idx].copy()))
+        st = pg.PgStats()
+        pg.perft_batch_device(d_b.data_ptr(), d_d.data_ptr(), len(idx), d_o.data_ptr(), graph=True,
+                              persistent=True, stats=st)
+        assert np.array_equal(d_o.cpu().numpy().view(np.uint64), g["totals"][idx]), k
+        seen.append((st.graph_captures, st.graph_replays))
+    assert seen == [(1, 0), (0, 1), (0, 1), (0, 1)]

@@ -130,3 +130,24 @@ def test_hbm_admission_binds_and_no_request_starves(pg):
     assert st["admissions_deferred"] > 0
     assert st["max_active"] >= 2
     assert 0 < st["pool_peak"] <= st["pool_capacity"] == 3200
+
+
+def test_server_persistent_waves_match_golden(pg):
+    """Waves run as one persistent launch each: every count equals the
+    reference's golden count, with requests arriving while others run."""
+    g3 = golden_npz("config3.npz")
+    g2 = golden_json("config2.json")
+    deep = pg.HexaBitBoardPosition(*words_of_hex(g2["board"]))
+    idx = np.arange(3, 4096, 37)
+    boards = g3["boards"][idx].copy().view(pg.BOARD_DTYPE).reshape(-1)
+    srv = pg.Server(hbm_budget_bytes=1 << 30, max_inflight=256, persistent=True)
+    try:
+        want = {srv.submit(deep, 7): g2["perft7"]}
+        for k, i in enumerate(idx):
+            want[srv.submit(pg.board_of(boards[k]), int(g3["depths"][i]))] = int(g3["totals"][i])
+            if k == 40:
+                time.sleep(0.01)
+        got = {rid: srv.wait(rid, timeout=300)[0] for rid in want}
+    finally:
+        srv.stop()
+    assert got == want
