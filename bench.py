@@ -299,6 +299,29 @@ def serve_leg(pg, rates, seconds, plain_rate):
     if stable:
         top = max(stable, key=lambda r: r["rate_req_s"])
         out["highest_sustained"] = {"rate_req_s": top["rate_req_s"], "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"]}
+    # the same kind of stream at the middle rate with each wave as one
+    # persistent launch (no per-level host round trips)
+    arrivals = np.cumsum(rng.exponential(1.0 / plain_rate, max_n))
+    n = int(np.searchsorted(arrivals, seconds))
+    srv = pg.Server(hbm_budget_bytes=8 << 30, persistent=True)
+    ids = []
+    t0 = time.perf_counter()
+    for i in range(n):
+        dt = t0 + arrivals[i] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        ids.append(srv.submit(pg.board_of(boards[i]), int(depths[i])))
+    res = [srv.wait(r, timeout=900) for r in ids]
+    wall = time.perf_counter() - t0
+    srv.stop()
+    lat = [l for _, l in res]
+    ref = pg.perft_batch(boards[:n], depths[:n])
+    assert [int(r) for r, _ in res] == [int(x) for x in ref], "persistent-wave counts differ"
+    check_n += n
+    out["persistent_waves"] = {"rate_req_s": plain_rate, "requests": n, "p50_ms": pct(lat, 50),
+                               "p99_ms": pct(lat, 99), "max_ms": max(lat) if lat else None,
+                               "leaves_per_s": sum(int(r) for r, _ in res) / wall,
+                               "path": "server with each wave as one persistent launch"}
     # the same kind of stream at the middle rate, served through the
     # transposition tables (they persist across requests)
     arrivals = np.cumsum(rng.exponential(1.0 / plain_rate, max_n))

@@ -269,9 +269,10 @@ template <int T> constexpr int min_blocks() { return (PG_LEAF_MIN_WARPS * 32 + T
 // queued children, one at a time.  A CTA's children normally fit one queue
 // window; when they do not, the later windows generate again.
 template <int S, class SL, int T, int QCAP>
-__device__ __forceinline__ void leaf_body(const LevelView& lv, u32 start, u32 n, u64* acc, u32* ticket, u32 max_rem,
-                                          unsigned char* pg_dyn_smem)
+__device__ __forceinline__ void leaf_body(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
+                                          u32 max_rem)
 {
+    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     using L = BlockSmem<SL, T, QCAP>;
     Pos* sb = reinterpret_cast<Pos*>(pg_dyn_smem + L::tables);
     u32* q = reinterpret_cast<u32*>(pg_dyn_smem + L::tables + L::boards);
@@ -359,9 +360,8 @@ template <int S, class SL, int T, int QCAP>
 __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
                                                             u32 max_rem)
 {
-    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     stage_tables<SL>();
-    leaf_body<S, SL, T, QCAP>(lv, start, n, acc, ticket, max_rem, pg_dyn_smem);
+    leaf_body<S, SL, T, QCAP>(lv, start, n, acc, ticket, max_rem);
 }
 
 // children of the nodes [a, b) of a level into the next level; offs is the
@@ -370,9 +370,9 @@ __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 s
 // slot and its parent's slot is written to parent_out
 template <int S, class SL, int T, int QCAP>
 __device__ __forceinline__ void expand_body(const LevelView& in, u32 start, u32 a, u32 b, const u64* offs,
-                                            const LevelView& out, u32* ticket, u32* parent_out,
-                                            unsigned char* pg_dyn_smem)
+                                            const LevelView& out, u32* ticket, u32* parent_out)
 {
+    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     using L = BlockSmem<SL, T, QCAP>;
     Pos* sb = reinterpret_cast<Pos*>(pg_dyn_smem + L::tables);
     u32* q = reinterpret_cast<u32*>(pg_dyn_smem + L::tables + L::boards);
@@ -435,9 +435,8 @@ template <int S, class SL, int T, int QCAP>
 __global__ void __launch_bounds__(T, min_blocks<T>()) k_expand(LevelView in, u32 start, u32 a, u32 b, const u64* __restrict__ offs,
                                               LevelView out, u32* ticket, u32* __restrict__ parent_out = nullptr)
 {
-    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     stage_tables<SL>();
-    expand_body<S, SL, T, QCAP>(in, start, a, b, offs, out, ticket, parent_out, pg_dyn_smem);
+    expand_body<S, SL, T, QCAP>(in, start, a, b, offs, out, ticket, parent_out);
 }
 
 }  // namespace pg

@@ -207,18 +207,15 @@ __device__ __forceinline__ void persist_plan(const u64* offs, u32 n, u64 cap, Pl
 }
 
 template <int S>
-__device__ __noinline__ void persist_leaf(const PersistArgs& A, int L, u32 start, u32 n, u32* ticket,
-                                          unsigned char* smem)
+__device__ __noinline__ void persist_leaf(const PersistArgs& A, int L, u32 start, u32 n, u32* ticket)
 {
-    leaf_body<S, SlKS, PERSIST_T, PERSIST_Q>(A.lv[L], start, n, A.acc, ticket, 2u, smem);
+    leaf_body<S, SlKS, PERSIST_T, PERSIST_Q>(A.lv[L], start, n, A.acc, ticket, 2u);
 }
 
 template <int S>
-__device__ __noinline__ void persist_expand(const PersistArgs& A, int L, u32 start, u32 a, u32 b, u32* ticket,
-                                            unsigned char* smem)
+__device__ __noinline__ void persist_expand(const PersistArgs& A, int L, u32 start, u32 a, u32 b, u32* ticket)
 {
-    expand_body<S, SlKS, PERSIST_T, PERSIST_Q>(A.lv[L], start, a, b, A.offs[L], A.lv[L + 1], ticket, nullptr,
-                                               smem);
+    expand_body<S, SlKS, PERSIST_T, PERSIST_Q>(A.lv[L], start, a, b, A.offs[L], A.lv[L + 1], ticket, nullptr);
 }
 
 template <int S>
@@ -237,7 +234,6 @@ struct PersistFrame {
 // A.acc[group]), two-ply leaf, Kogge-Stone sliders, PERSIST_T threads.
 __global__ void __launch_bounds__(PERSIST_T, min_blocks<PERSIST_T>()) k_persist(PersistArgs A)
 {
-    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     PersistCtl* ctl = A.ctl;
     // phase 0: roots into level 0, white-to-move first (k_partition_roots)
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
@@ -283,8 +279,8 @@ __global__ void __launch_bounds__(PERSIST_T, min_blocks<PERSIST_T>()) k_persist(
                         if (blockIdx.x == 0 && threadIdx.x == 0) persist_fail(A, ERR_PLAN_OVERFLOW);
                         return;
                     }
-                    if (f.side) persist_leaf<1>(A, L, f.start, f.n, t, pg_dyn_smem);
-                    else persist_leaf<0>(A, L, f.start, f.n, t, pg_dyn_smem);
+                    if (f.side) persist_leaf<1>(A, L, f.start, f.n, t);
+                    else persist_leaf<0>(A, L, f.start, f.n, t);
                 }
                 if (f.maxrem <= 2) {
                     --top;
@@ -332,8 +328,8 @@ __global__ void __launch_bounds__(PERSIST_T, min_blocks<PERSIST_T>()) k_persist(
                     if (blockIdx.x == 0 && threadIdx.x == 0) persist_fail(A, ERR_PLAN_OVERFLOW);
                     return;
                 }
-                if (f.side) persist_expand<1>(A, L, f.start, a, b, t, pg_dyn_smem);
-                else persist_expand<0>(A, L, f.start, a, b, t, pg_dyn_smem);
+                if (f.side) persist_expand<1>(A, L, f.start, a, b, t);
+                else persist_expand<0>(A, L, f.start, a, b, t);
                 if (!grid_barrier(ctl, A.err)) return;
                 stack[top + 1] = PersistFrame{0u, (u32)children, 1 - f.side, max(f.minrem, 3) - 1, f.maxrem - 1,
                                               0xFFFFFFFFu};

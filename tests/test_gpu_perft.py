@@ -247,8 +247,8 @@ def test_persistent_graph_replays_any_contents(pg):
     replay the same graph and give their own golden counts."""
     import torch
     g = golden_npz("config3.npz")
-    a = np.arange(0, 4096, 13)
-    b = np.arange(5, 4096, 13)[:len(a)]
+    b = np.arange(5, 4096, 13)
+    a = np.arange(0, 4096, 13)[:len(b)]
     sel = [a, b]
     assert g["depths"][a].max() == g["depths"][b].max()
     d_b = torch.from_numpy(g["boards"][a].copy().view(np.uint8)).cuda()
