@@ -41,7 +41,7 @@ def _sources():
 def _deps():
     deps = _sources()
     for f in os.listdir(CSRC):
-        if f.endswith((".cuh", ".h")):
+        if f.endswith((".cuh", ".h", ".inc")):
             deps.append(os.path.join(CSRC, f))
     deps.append(os.path.join(ROOT, "include", "perft_gb300.h"))
     deps.append(os.path.abspath(__file__))

@@ -262,106 +262,26 @@ template <class SL, int T, int QCAP> struct BlockSmem {
 #endif
 template <int T> constexpr int min_blocks() { return (PG_LEAF_MIN_WARPS * 32 + T - 1) / T; }
 
-// the last plies of every node with remaining depth <= 2, inside one CTA.
-// Each thread takes one node and counts its moves; the CTA scans the counts;
-// each thread writes its node's moves into the shared queue as (node, move,
-// landing piece, en-passant bit) entries; then every thread makes and counts
-// queued children, one at a time.  A CTA's children normally fit one queue
-// window; when they do not, the later windows generate again.
+// the last plies of every node with remaining depth <= 2, inside one CTA
+// (pg_leaf_body.inc).  The kernel includes the statements in its own body,
+// not through this function: with the arguments left in the parameter space
+// the compiler keeps more registers for the count (measured 0.5-0.9% faster
+// than calling the inlined function).
 template <int S, class SL, int T, int QCAP>
 __device__ __forceinline__ void leaf_body(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
                                           u32 max_rem)
 {
     extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
-    using L = BlockSmem<SL, T, QCAP>;
-    Pos* sb = reinterpret_cast<Pos*>(pg_dyn_smem + L::tables);
-    u32* q = reinterpret_cast<u32*>(pg_dyn_smem + L::tables + L::boards);
-    u32* sg = q + QCAP;
-    __shared__ u32 s_warp[T / 32];
-    __shared__ u32 s_chunk;
-    const int tid = threadIdx.x;
-    GroupAcc ga;
-    for (;;) {
-        if (tid == 0) s_chunk = atomicAdd(ticket, 1u);
-        __syncthreads();
-        const u64 c0 = (u64)s_chunk * T;
-        if (c0 >= n) break;
-        const u64 i = c0 + tid;
-        Pos b{0, 0, 0, 0, 0, 0};
-        u32 grp = 0, c = 0;
-        // the Kogge-Stone and hybrid policies count the node from the same
-        // analysis the generator uses: made once, kept across the block scan
-        constexpr bool kFacts = SL::kId == 0 || SL::kId == 3;
-        KsFacts<S> f{};
-        if (i < n) {
-            b = load_board(lv, start + i);
-            grp = lv.grp[start + i];
-            const int rem = lv.rem[start + i];
-            if (rem == 2 && max_rem >= 2) {
-                if constexpr (kFacts) {
-                    f = ks_facts<S>(b);
-                    c = count_from_facts<S, SL::kId == 3>(b, f);
-                } else {
-                    c = count_moves<S, SL>(b);
-                }
-            } else if (rem == 1) {
-                ga.add(acc, grp, count_moves<S, SL>(b));
-            } else if (rem == 0) {
-                ga.add(acc, grp, 1);
-            }
-        }
-        sb[tid] = b;
-        sg[tid] = grp;
-        u32 total;
-        const u32 off = block_excl_scan<T>(c, total, s_warp);
-        // make and count the queued children of window [lo, hi)
-        auto children = [&](u32 lo, u32 hi) {
-            __syncthreads();
-            const u32 m = hi - lo;
-            for (u32 e = tid; e < m; e += T) {
-                const u32 ent = q[e];
-                const u32 p = (ent >> 16) & (T - 1);  // in bounds even if a queue slot was left unwritten
-                Pos ch = sb[p];
-                make_child<S>(ch, (u16)(ent & 0xFFFFu), (ent >> 25) & 15u);
-                ga.add(acc, sg[p], count_moves<1 - S, SL>(ch));
-            }
-            __syncthreads();
-        };
-        // the first window generates from the kept analysis; later ones (rare:
-        // more children than the queue holds) make it again
-        if (total) {
-            const u32 hi = min((u32)QCAP, total);
-            if (total <= (u32)QCAP) {  // one window: no position checks
-                if (c) {
-                    QEmitAll e{q, off, (u32)tid << 16};
-                    if constexpr (kFacts) gen_from_facts<S>(b, f, e);
-                    else gen_leaf<S>(b, e);
-                }
-            } else if (c && off < hi) {
-                QEmit e{q, off, 0u, hi, (u32)tid << 16};
-                if constexpr (kFacts) gen_from_facts<S>(b, f, e);
-                else gen_leaf<S>(b, e);
-            }
-            children(0u, hi);
-        }
-        for (u32 lo = QCAP; lo < total; lo += QCAP) {
-            const u32 hi = min(lo + (u32)QCAP, total);
-            if (c && off < hi && off + c > lo) {
-                QEmit e{q, off, lo, hi, (u32)tid << 16};
-                gen_leaf<S>(b, e);
-            }
-            children(lo, hi);
-        }
-    }
-    ga.flush_warp(acc);
+#include "pg_leaf_body.inc"
 }
 
 template <int S, class SL, int T, int QCAP>
 __global__ void __launch_bounds__(T, min_blocks<T>()) k_leaf(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
                                                             u32 max_rem)
 {
+    extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
     stage_tables<SL>();
-    leaf_body<S, SL, T, QCAP>(lv, start, n, acc, ticket, max_rem);
+#include "pg_leaf_body.inc"
 }
 
 // children of the nodes [a, b) of a level into the next level; offs is the

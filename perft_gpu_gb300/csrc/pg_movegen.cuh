@@ -583,7 +583,16 @@ __device__ __forceinline__ u32 count_moves_ks1(const Pos& b)
         n -= popc(att & tgt & ~(line & ~chk_all));
     }
 
-    for (u64 s = b.n & mine & ~pinned; s; s &= s - 1) n += popc(__ldg(&g_knight[lsb(s)]) & tgt);
+    {
+        // the first two knights without a loop (fewer instructions and no
+        // divergence on the usual one or two); a third (promotions) loops
+        const u64 kn = b.n & mine & ~pinned;
+        const u64 k1 = kn & (0ull - kn), rest = kn ^ k1;
+        const u64 k2 = rest & (0ull - rest);
+        n += popc(__ldg(&g_knight[sq_of(k1)]) & tgt & (k1 ? ~0ull : 0ull));
+        n += popc(__ldg(&g_knight[sq_of(k2)]) & tgt & (k2 ? ~0ull : 0ull));
+        for (u64 s = rest ^ k2; s; s &= s - 1) n += popc(__ldg(&g_knight[lsb(s)]) & tgt);
+    }
 
     // pawns, castling and en passant as in count_from_facts
     const u64 myp = pawns & mine;
