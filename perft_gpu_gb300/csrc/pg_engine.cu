@@ -132,7 +132,7 @@ int launch_scan(const u32* cnt, u32 n, u64* offs)
 // level buffers
 // ---------------------------------------------------------------------------
 
-static constexpr u64 NODE_BYTES = 48 + 4 + 1 + 4 + 8;
+static constexpr u64 NODE_BYTES = LEVEL_NODE_BYTES;
 
 u64 level_cap_max()
 {

@@ -13,6 +13,9 @@
 namespace pg {
 
 constexpr int MAX_LEVELS = 16;
+// device bytes per node of a level buffer: the board (48), group id (4),
+// remaining depth (1), child count (4) and scanned offset (8)
+constexpr u64 LEVEL_NODE_BYTES = 48 + 4 + 1 + 4 + 8;
 constexpr u32 MAX_CHUNKS = 2048;      // greedy chunks planned per expansion
 constexpr u32 MAX_TICKETS = 1 << 16;  // dynamic-scheduling counters per call
 

@@ -302,6 +302,25 @@ static int ensure_tables(u64 bytes)
     return PG_OK;
 }
 
+// per node of a level in the TT driver, beside the level buffer: both key
+// words, the count, the parent slot and the duplicate index (32 B), and at
+// most four slots of the level's duplicate table (12 B each: the table has a
+// power-of-two size of at least two slots per node)
+constexpr u64 TT_NODE_BYTES = 32 + 4 * 12;
+
+// nodes a level of the TT driver holds: a quarter of the HBM budget left
+// beside the tables, over the level buffer's and the TT metadata's bytes
+// per node (the same share as level_cap_max gives the driver without TT)
+static u64 tt_level_cap()
+{
+    Engine& E = engine();
+    const u64 avail = E.budget > g_tt.pool_bytes ? E.budget - g_tt.pool_bytes : E.budget / 4;
+    const u64 cap = std::min<u64>(avail / (LEVEL_NODE_BYTES + TT_NODE_BYTES) / 4, level_cap_max());
+    return std::max<u64>(cap, 1u << 16);
+}
+
+// sized to the nodes asked for (a multiple of 65,536), not the next power
+// of two: at the largest levels the rounding alone would double the bytes
 static int ensure_level_tt(int L, u64 need)
 {
     LevelTT& t = g_tt.lv[L];
@@ -311,9 +330,9 @@ static int ensure_level_tt(int L, u64 need)
         cudaFree(t.block);
         t = LevelTT{};
     }
-    u64 cap = 1 << 16;
-    while (cap < need) cap <<= 1;
-    const u64 dd = cap * 2;
+    const u64 cap = std::max<u64>(1u << 16, (need + 65535) & ~65535ull);
+    u64 dd = 1u << 17;
+    while (dd < 2 * cap) dd <<= 1;
     const u64 bytes = cap * (8 + 8 + 8 + 4 + 4) + dd * (8 + 4) + 1024;
     void* blk = nullptr;
     cudaError_t e = cudaMalloc(&blk, bytes);
@@ -362,7 +381,7 @@ static int run_range_tt(const Variant& v, int L, u32 start, u32 n, int side, int
     if (maxrem < 3) return PG_OK;
     TT_TRY(launch_count(v, side, lb.v, start, n, lb.cnt));
     TT_TRY(launch_scan(lb.cnt, n, lb.offs));
-    const u64 cap_next = level_cap_max();
+    const u64 cap_next = tt_level_cap();
     k_plan<<<1, 32, 0, E.stream>>>(lb.offs, n, cap_next, E.plan_dev, E.err);
     TT_CUDA(cudaGetLastError());
     TT_CUDA(cudaMemcpyAsync(E.plan_host, E.plan_dev, sizeof(PlanOut), cudaMemcpyDeviceToHost, E.stream));
