@@ -151,8 +151,12 @@ int ensure_level(int L, u64 need)
     }
     LevelBuf& lb = E.lv[L];
     if (lb.cap >= need) return PG_OK;
-    u64 cap = 1u << 16;
-    while (cap < need) cap <<= 1;
+    // rounded up to an eighth of the next power of two (at most 12.5% over
+    // the need, so a level regrows rarely without doubling its bytes)
+    u64 p2 = 1u << 16;
+    while (p2 < need) p2 <<= 1;
+    const u64 step = std::max<u64>(p2 / 8, 1u << 16);
+    u64 cap = (need + step - 1) / step * step;
     cap = std::min(cap, std::max(level_cap_max(), need));
     E.alloc_gen++;
     if (lb.block) {

@@ -83,7 +83,12 @@ __device__ __forceinline__ u64 dd_key(u64 h, u32 rem)
     const u64 k = h ^ (0x9E3779B97F4A7C15ull * (rem + 1));
     return k ? k : 1;
 }
-__device__ __forceinline__ u32 dd_slot(u64 k, u64 mask) { return (u32)(((k >> 23) ^ (k >> 41) ^ k) & mask); }
+// slot of a digest in a table of `slots` entries (any size): the high word of
+// digest x slots, after a multiply that spreads every digest bit upward
+__device__ __forceinline__ u32 dd_slot(u64 k, u64 slots)
+{
+    return (u32)__umul64hi(k * 0xD6E8FEB86659FD93ull ^ (k >> 32), slots);
+}
 
 // Adds a per-thread count into *dst with one global atomic per CTA (the
 // threads of a warp are summed by a warp reduction, the warps in shared
@@ -100,7 +105,7 @@ __device__ __forceinline__ void block_count_add(u64* dst, u32 v)
 }
 
 // key, TT probe, and first claim of the level's duplicate table
-static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TTSet tt, u64 dd_mask, u64* counters)
+static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TTSet tt, u64 dd_slots, u64* counters)
 {
     __shared__ ulonglong2 z[ZOBRIST_KEYS];
     for (int i = threadIdx.x; i < ZOBRIST_KEYS; i += blockDim.x) z[i] = g_zobrist[i];
@@ -129,7 +134,7 @@ static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TT
             }
         }
         const u64 k = dd_key(h.x, rem);
-        const u32 s = dd_slot(k, dd_mask);
+        const u32 s = dd_slot(k, dd_slots);
         const u64 prev = atomicCAS(&lt.dd_hash[s], 0ull, k);
         if (prev == 0 || prev == k) atomicMin(&lt.dd_idx[s], idx);
     }
@@ -143,7 +148,7 @@ static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TT
 // slot's digest; a node whose full key or depth differs from the claimant's
 // (a digest collision) keeps its own work.  Claimants are never marked here,
 // so their depth and key are stable while others compare against them.
-static __global__ void k_tt_dedup(LevelView lv, u32 start, u32 n, LevelTT lt, u64 dd_mask)
+static __global__ void k_tt_dedup(LevelView lv, u32 start, u32 n, LevelTT lt, u64 dd_slots)
 {
     for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const u32 idx = start + i;
@@ -151,7 +156,7 @@ static __global__ void k_tt_dedup(LevelView lv, u32 start, u32 n, LevelTT lt, u6
         if (rem < TT_MIN_DEPTH || rem >= REM_DEAD) continue;
         const u64 h0 = lt.hash0[idx];
         const u64 k = dd_key(h0, rem);
-        const u32 s = dd_slot(k, dd_mask);
+        const u32 s = dd_slot(k, dd_slots);
         if (lt.dd_hash[s] == k) {
             const u32 rep = lt.dd_idx[s];
             if (rep != idx && lt.hash0[rep] == h0 && lt.hash1[rep] == lt.hash1[idx] && lv.rem[rep] == rem) {
@@ -303,10 +308,9 @@ static int ensure_tables(u64 bytes)
 }
 
 // per node of a level in the TT driver, beside the level buffer: both key
-// words, the count, the parent slot and the duplicate index (32 B), and at
-// most four slots of the level's duplicate table (12 B each: the table has a
-// power-of-two size of at least two slots per node)
-constexpr u64 TT_NODE_BYTES = 32 + 4 * 12;
+// words, the count, the parent slot and the duplicate index (32 B), and two
+// slots of the level's duplicate table (12 B each)
+constexpr u64 TT_NODE_BYTES = 32 + 2 * 12;
 
 // nodes a level of the TT driver holds: a quarter of the HBM budget left
 // beside the tables, over the level buffer's and the TT metadata's bytes
@@ -331,8 +335,7 @@ static int ensure_level_tt(int L, u64 need)
         t = LevelTT{};
     }
     const u64 cap = std::max<u64>(1u << 16, (need + 65535) & ~65535ull);
-    u64 dd = 1u << 17;
-    while (dd < 2 * cap) dd <<= 1;
+    const u64 dd = 2 * cap;
     const u64 bytes = cap * (8 + 8 + 8 + 4 + 4) + dd * (8 + 4) + 1024;
     void* blk = nullptr;
     cudaError_t e = cudaMalloc(&blk, bytes);
@@ -368,13 +371,13 @@ static int run_range_tt(const Variant& v, int L, u32 start, u32 n, int side, int
     if (n == 0) return PG_OK;
     LevelBuf& lb = E.lv[L];
     LevelTT& lt = g_tt.lv[L];
-    u64 dd = 1024;
-    while (dd < 2ull * n) dd <<= 1;
-    dd = std::min(dd, lt.dd_cap);
+    // two duplicate-table slots per node of the range (the table is sized for
+    // the level's capacity)
+    const u64 dd = std::min(std::max<u64>(1024, 2ull * n), lt.dd_cap);
     TT_CUDA(cudaMemsetAsync(lt.dd_hash, 0, dd * 8, E.stream));
     TT_CUDA(cudaMemsetAsync(lt.dd_idx, 0xFF, dd * 4, E.stream));
-    k_tt_probe<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, g_tt.active, dd - 1, g_tt.counters);
-    k_tt_dedup<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, dd - 1);
+    k_tt_probe<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, g_tt.active, dd, g_tt.counters);
+    k_tt_dedup<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, dd);
     TT_CUDA(cudaGetLastError());
     E.st.launches += 2;
     if (minrem <= 2) TT_TRY(launch_leaf(v, side, lb.v, start, n, lt.acc));
