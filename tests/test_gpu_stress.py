@@ -36,3 +36,15 @@ def test_random_playouts_mixed_depths_with_tt(pg, orc):
     got = pg.perft_batch(boards, depths, use_tt=True, tt_bytes=256 << 20)
     pg.tt_clear()
     assert np.array_equal(got, want)
+
+
+def test_random_playouts_persistent_and_dedup_match_oracle(pg, orc):
+    """The persistent launch and the in-level duplicate pass on fresh
+    playouts of mixed depth, against the oracle."""
+    boards, depths = pg.random_playouts(14, 20000, 0, 120, 1, 0, 4, with_depths=True)
+    want, _ = orc.perft_batch(boards, depths, os.cpu_count() or 1)
+    got = pg.perft_batch(boards, depths, persistent=True)
+    bad = np.nonzero(got != want)[0]
+    assert len(bad) == 0, ("persistent", int(bad[0]), int(got[bad[0]]), int(want[bad[0]]))
+    got = pg.perft_batch(boards, depths, use_tt="dedup")
+    assert np.array_equal(got, want)
