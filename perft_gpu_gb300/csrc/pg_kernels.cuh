@@ -266,10 +266,10 @@ template <int T> constexpr int min_blocks() { return (PG_LEAF_MIN_WARPS * 32 + T
 // (pg_leaf_body.inc).  The kernel includes the statements in its own body,
 // not through this function: with the arguments left in the parameter space
 // the compiler keeps more registers for the count (measured 0.5-0.9% faster
-// than calling the inlined function).
-template <int S, class SL, int T, int QCAP>
-__device__ __forceinline__ void leaf_body(LevelView lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket,
-                                          u32 max_rem)
+// than calling the inlined function).  LV is LevelView or any type with the
+// same grp[] / rem[] subscripts and a load_board overload.
+template <int S, class SL, int T, int QCAP, class LV>
+__device__ __forceinline__ void leaf_body(LV lv, u32 start, u32 n, u64* __restrict__ acc, u32* ticket, u32 max_rem)
 {
     extern __shared__ __align__(16) unsigned char pg_dyn_smem[];
 #include "pg_leaf_body.inc"
