@@ -206,39 +206,10 @@ __device__ __forceinline__ void persist_plan(const u64* offs, u32 n, u64 cap, Pl
     plan->total = offs[n];
 }
 
-// The level view of the running leaf phase, in shared memory.  The leaf
-// statements read its pointers at each use through PhaseLevel (once per
-// parent node, with volatile loads the compiler cannot hoist), so they take
-// no registers in the child loop, where the count needs all 128: held in
-// registers they made the leaf phase 4-5% slower than k_leaf, which reads
-// them from its parameter bank.
-static __shared__ LevelView s_phase_lv;
-
-template <class P> __device__ __forceinline__ P phase_ptr(P const* p) { return *(P const volatile*)p; }
-struct PhaseGrp {
-    __device__ __forceinline__ u32 operator[](u64 i) const { return phase_ptr(&s_phase_lv.grp)[i]; }
-};
-struct PhaseRem {
-    __device__ __forceinline__ unsigned char operator[](u64 i) const { return phase_ptr(&s_phase_lv.rem)[i]; }
-};
-struct PhaseLevel {
-    PhaseGrp grp;
-    PhaseRem rem;
-};
-__device__ __forceinline__ Pos load_board(const PhaseLevel&, u64 i)
-{
-    const LevelView v{phase_ptr(&s_phase_lv.pl0), phase_ptr(&s_phase_lv.pl1), phase_ptr(&s_phase_lv.pl2), nullptr,
-                      nullptr};
-    return load_board(v, i);
-}
-
 template <int S>
 __device__ __noinline__ void persist_leaf(const PersistArgs& A, int L, u32 start, u32 n, u32* ticket)
 {
-    __syncthreads();  // the previous phase's readers of s_phase_lv are done
-    if (threadIdx.x == 0) s_phase_lv = A.lv[L];
-    __syncthreads();
-    leaf_body<S, SlKS, PERSIST_T, PERSIST_Q>(PhaseLevel{}, start, n, A.acc, ticket, 2u);
+    leaf_body<S, SlKS, PERSIST_T, PERSIST_Q>(A.lv[L], start, n, A.acc, ticket, 2u);
 }
 
 template <int S>
