@@ -206,8 +206,10 @@ __device__ __forceinline__ void persist_plan(const u64* offs, u32 n, u64 cap, Pl
     plan->total = offs[n];
 }
 
+// inlined into the kernel: as a called function the leaf phase ran 4-5%
+// slower than k_leaf (measured), inlined 1.3%
 template <int S>
-__device__ __noinline__ void persist_leaf(const PersistArgs& A, int L, u32 start, u32 n, u32* ticket)
+__device__ __forceinline__ void persist_leaf(const PersistArgs& A, int L, u32 start, u32 n, u32* ticket)
 {
     leaf_body<S, SlKS, PERSIST_T, PERSIST_Q>(A.lv[L], start, n, A.acc, ticket, 2u);
 }
