@@ -206,8 +206,8 @@ __device__ __forceinline__ void persist_plan(const u64* offs, u32 n, u64 cap, Pl
     plan->total = offs[n];
 }
 
-// inlined into the kernel: as a called function the leaf phase ran 4-5%
-// slower than k_leaf (measured), inlined 1.3%
+// the phases are inlined into the kernel: as called functions the leaf phase
+// ran 4-5% slower than k_leaf (measured), inlined about 1%
 template <int S>
 __device__ __forceinline__ void persist_leaf(const PersistArgs& A, int L, u32 start, u32 n, u32* ticket)
 {
@@ -215,13 +215,13 @@ __device__ __forceinline__ void persist_leaf(const PersistArgs& A, int L, u32 st
 }
 
 template <int S>
-__device__ __noinline__ void persist_expand(const PersistArgs& A, int L, u32 start, u32 a, u32 b, u32* ticket)
+__device__ __forceinline__ void persist_expand(const PersistArgs& A, int L, u32 start, u32 a, u32 b, u32* ticket)
 {
     expand_body<S, SlKS, PERSIST_T, PERSIST_Q>(A.lv[L], start, a, b, A.offs[L], A.lv[L + 1], ticket, nullptr);
 }
 
 template <int S>
-__device__ __noinline__ void persist_count(const PersistArgs& A, int L, u32 start, u32 n)
+__device__ __forceinline__ void persist_count(const PersistArgs& A, int L, u32 start, u32 n)
 {
     count_level_body<S, SlKS>(A.lv[L], start, n, A.cnt[L], 3u);
 }
