@@ -118,3 +118,27 @@ def test_tt_full_key_separates_positions_in_one_level(pg):
     for _ in range(2):
         assert np.array_equal(pg.perft_batch(boards, depths, use_tt=True, tt_bytes=1 << 20), ref)
     pg.tt_clear()
+
+
+def test_tt_chunked_levels_small_budget(pg):
+    """A small HBM budget makes the TT driver split its levels into many
+    chunks sized with the per-node TT metadata (later chunks then hit the
+    tables earlier chunks stored): counts still equal the golden counts and
+    the no-TT counts."""
+    fens = {f["name"]: f for f in golden_json("fens.json")}
+    pg.shutdown()
+    pg.init(hbm_budget_bytes=256 << 20)
+    try:
+        b = pg.board_from_fen(fens["position2"]["fen"])
+        pg.tt_clear()
+        st = pg.PgStats()
+        assert pg.perft(b, 5, use_tt=True, tt_bytes=16 << 20, stats=st) == fens["position2"]["perft"]["5"]
+        assert st.tt_stores > 0
+        g = golden_npz("config4_d5.npz")
+        boards = g["boards"][:64].copy().view(pg.BOARD_DTYPE).reshape(-1)
+        for mode in (True, "dedup"):
+            assert np.array_equal(pg.perft_batch(boards, [5] * 64, use_tt=mode, tt_bytes=16 << 20), g["totals"][:64])
+    finally:
+        pg.tt_clear()
+        pg.shutdown()
+        pg.init()
