@@ -23,8 +23,9 @@ workload every step (every 16th position, the sample of the cpu_baseline leg).
 
 --profile-case N runs every (4096/N)-th position of the workload once
 (Kogge-Stone sliders, 128-thread CTAs, two-ply leaf: the autotuner's choice
-for the depths that hold most leaves), checks the counts and prints one JSON
-line: the small case of the same kernels for ncu captures.
+for the depths that hold most leaves; with --persistent as one persistent
+launch), checks the counts and prints one JSON line: the small case of the
+same kernels for ncu captures.
 """
 from __future__ import annotations
 
@@ -757,9 +758,13 @@ def run_profile_case(args):
                                         WORKLOAD["depth_lo"], WORKLOAD["depth_hi"], with_depths=True)
     idx = np.arange(0, len(boards), max(1, len(boards) // args.profile_case))
     st = pg.PgStats()
-    out = pg.perft_batch(boards[idx], depths[idx], slider="ks", block_size=128, leaf_plies=2, stats=st)
+    if args.persistent:
+        out = pg.perft_batch(boards[idx], depths[idx], persistent=True, stats=st)
+    else:
+        out = pg.perft_batch(boards[idx], depths[idx], slider="ks", block_size=128, leaf_plies=2, stats=st)
     ok = bool(np.array_equal(out, g[0][idx])) if g is not None else None
-    print(json.dumps({"profile_case": len(idx), "positions": "every %dth of the batched workload" % (len(boards) // len(idx)),
+    print(json.dumps({"profile_case": len(idx), "persistent": bool(args.persistent),
+                      "positions": "every %dth of the batched workload" % (len(boards) // len(idx)),
                       "leaves": int(out.sum()), "verified_bit_exact": ok,
                       "leaf_kernel_launches": st.leaf_kernel_launches, "leaf_parent_nodes": st.leaf_parent_nodes,
                       "leaf_kernel_ms": st.leaf_kernel_ms, "device_ms": st.device_ms, "launches": st.launches}))
@@ -785,6 +790,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=8.0)
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run N positions of the workload once and exit (small case for ncu)")
+    ap.add_argument("--persistent", action="store_true",
+                    help="with --profile-case: as one persistent launch")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
