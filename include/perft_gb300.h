@@ -196,6 +196,14 @@ int pg_tt_clear(void);
  * The half-move clock is not part of the key.  Host code: needs no GPU and
  * no pg_init. */
 int pg_zobrist_key(const pg_board *pos, uint64_t key[2]);
+/* The key of pos from the key of another board `from`: from_key XOR the
+ * features in which the two boards differ (for a parent and its child, the
+ * squares the move changed, the castling rights and en-passant files, the
+ * side to move) -- the incremental update of the reference's
+ * makeMove<c, true> (MoveGeneratorBitboard.h:3575-3836), the code the probe
+ * kernel runs below the root level.  Equals pg_zobrist_key(pos) whenever
+ * from_key == pg_zobrist_key(from).  Host code: needs no GPU and no pg_init. */
+int pg_zobrist_key_from(const pg_board *from, const uint64_t from_key[2], const pg_board *pos, uint64_t key[2]);
 /* The 32-byte table entry of a key and its count, and the check a probe
  * makes (the reference's XOR-verified entries, chess.h:454-482 and the probe
  * of perft_bb.h:690-693, widened to verify all 128 key bits):

@@ -178,6 +178,7 @@ _SIGNATURES = {
     "pg_perft_split": [_BP, ctypes.c_int, ctypes.c_int, _U16P, _U64P, _U32P, _OP],
     "pg_selftest": [ctypes.c_int],
     "pg_zobrist_key": [_BP, _U64P],
+    "pg_zobrist_key_from": [_BP, _U64P, _BP, _U64P],
     "pg_tt_entry_pack": [_U64P, ctypes.c_uint64, _U64P],
     "pg_tt_entry_match": [_U64P, _U64P, ctypes.POINTER(ctypes.c_int), _U64P],
     "pg_perft_batch_noalloc": [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
@@ -391,6 +392,17 @@ def zobrist_key(pos: HexaBitBoardPosition) -> tuple[int, int]:
     k = (ctypes.c_uint64 * 2)()
     _check(load_library().pg_zobrist_key(ctypes.byref(pos), k))
     return k[0], k[1]
+
+
+def zobrist_key_from(src: HexaBitBoardPosition, src_key: tuple[int, int],
+                     pos: HexaBitBoardPosition) -> tuple[int, int]:
+    """The key of `pos` updated from the key of `src` by the features the two
+    boards differ in (the incremental update the probe kernel makes from a
+    parent to its child)."""
+    k = (ctypes.c_uint64 * 2)(*src_key)
+    out = (ctypes.c_uint64 * 2)()
+    _check(load_library().pg_zobrist_key_from(ctypes.byref(src), k, ctypes.byref(pos), out))
+    return out[0], out[1]
 
 
 def tt_entry_pack(key: tuple[int, int], count: int) -> tuple[int, int, int, int]:

@@ -104,8 +104,22 @@ __device__ __forceinline__ void block_count_add(u64* dst, u32 v)
     if (threadIdx.x == 0 && s_sum) atomicAdd(dst, (u64)s_sum);
 }
 
-// key, TT probe, and first claim of the level's duplicate table
-static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TTSet tt, u64 dd_slots, u64* counters)
+// the parent level of a level below the root, as the probe reads it: its
+// boards and keys, and each node's parent slot (parent null at the root level)
+struct ParentKeys {
+    LevelView lv;
+    const u64* hash0;
+    const u64* hash1;
+    const u32* parent;
+};
+
+// key, TT probe, and first claim of the level's duplicate table.  Below the
+// root level a node's key is its parent's key updated by the features the
+// move changed (the parent was probed one level up: a child that reaches
+// the probe has remaining depth >= TT_MIN_DEPTH, so its parent had more
+// and its key was written); at the root level the key is computed in full.
+static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, ParentKeys pk, TTSet tt, u64 dd_slots,
+                                  u64* counters)
 {
     __shared__ ulonglong2 z[ZOBRIST_KEYS];
     for (int i = threadIdx.x; i < ZOBRIST_KEYS; i += blockDim.x) z[i] = g_zobrist[i];
@@ -118,7 +132,14 @@ static __global__ void k_tt_probe(LevelView lv, u32 start, u32 n, LevelTT lt, TT
         lt.dup[idx] = NO_DUP;
         if (rem < TT_MIN_DEPTH || rem >= REM_DEAD) continue;
         const Pos b = load_board(lv, idx);
-        const ulonglong2 h = zobrist128(&b.w, z);
+        ulonglong2 h;
+        if (pk.parent) {
+            const u32 p = pk.parent[idx];
+            const Pos pb = load_board(pk.lv, p);
+            h = zobrist128_from(&pb.w, make_ulonglong2(pk.hash0[p], pk.hash1[p]), &b.w, z);
+        } else {
+            h = zobrist128(&b.w, z);
+        }
         lt.hash0[idx] = h.x;
         lt.hash1[idx] = h.y;
         if (rem <= TT_MAX_DEPTH && tt.tab[rem]) {
@@ -376,7 +397,9 @@ static int run_range_tt(const Variant& v, int L, u32 start, u32 n, int side, int
     const u64 dd = std::min(std::max<u64>(1024, 2ull * n), lt.dd_cap);
     TT_CUDA(cudaMemsetAsync(lt.dd_hash, 0, dd * 8, E.stream));
     TT_CUDA(cudaMemsetAsync(lt.dd_idx, 0xFF, dd * 4, E.stream));
-    k_tt_probe<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, g_tt.active, dd, g_tt.counters);
+    ParentKeys pk{};
+    if (L > 0) pk = {E.lv[L - 1].v, g_tt.lv[L - 1].hash0, g_tt.lv[L - 1].hash1, lt.parent};
+    k_tt_probe<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, pk, g_tt.active, dd, g_tt.counters);
     k_tt_dedup<<<small_grid(n), 256, 0, E.stream>>>(lb.v, start, n, lt, dd);
     TT_CUDA(cudaGetLastError());
     E.st.launches += 2;
@@ -645,18 +668,38 @@ using namespace pg;
 
 extern "C" {
 
+static const ulonglong2* host_key_table()
+{
+    static ulonglong2 keys[ZOBRIST_KEYS];
+    static const bool made = (zobrist_key_table(keys), true);
+    (void)made;
+    return keys;
+}
+
 int pg_zobrist_key(const pg_board* pos, uint64_t key[2])
 {
     if (!pos || !key) {
         set_error("null argument");
         return PG_ERR_INVALID_ARGUMENT;
     }
-    static ulonglong2 keys[ZOBRIST_KEYS];
-    static const bool made = (zobrist_key_table(keys), true);
-    (void)made;
     u64 w[6];
     memcpy(w, pos, sizeof(w));
-    const ulonglong2 h = zobrist128(w, keys);
+    const ulonglong2 h = zobrist128(w, host_key_table());
+    key[0] = h.x;
+    key[1] = h.y;
+    return PG_OK;
+}
+
+int pg_zobrist_key_from(const pg_board* from, const uint64_t from_key[2], const pg_board* pos, uint64_t key[2])
+{
+    if (!from || !from_key || !pos || !key) {
+        set_error("null argument");
+        return PG_ERR_INVALID_ARGUMENT;
+    }
+    u64 pw[6], cw[6];
+    memcpy(pw, from, sizeof(pw));
+    memcpy(cw, pos, sizeof(cw));
+    const ulonglong2 h = zobrist128_from(pw, make_ulonglong2(from_key[0], from_key[1]), cw, host_key_table());
     key[0] = h.x;
     key[1] = h.y;
     return PG_OK;

@@ -104,6 +104,61 @@ __host__ __device__ __forceinline__ ulonglong2 zobrist128(const u64* bw, const u
     return make_ulonglong2(h0, h1);
 }
 
+// The key of board cw from the key kp of board pw: kp XOR the features in
+// which the two boards differ.  For a parent and its child that is the
+// squares the move changed (two to four), the castling rights it cleared,
+// the old and new en-passant file and the side to move -- the update the
+// reference applies while making a move (makeMove<c, true>,
+// MoveGeneratorBitboard.h:3575-3836), taken here from the two boards instead
+// of from the move.  XOR is linear over the feature sets, so the result
+// equals zobrist128(cw) for any two boards; only the work depends on how
+// many features differ.  A key (1, 0) may stand for the raw key 0 (the
+// empty-slot remap above), so from such a key the board is keyed in full.
+__host__ __device__ __forceinline__ ulonglong2 zobrist128_from(const u64* pw, ulonglong2 kp, const u64* cw,
+                                                               const ulonglong2* z)
+{
+    if (kp.x == 1 && kp.y == 0) return zobrist128(cw, z);
+    const u64 pp = pw[1] & 0x00FFFFFFFFFFFF00ull, cp = cw[1] & 0x00FFFFFFFFFFFF00ull;
+    const u64 ps[6] = {pp, pw[2], pw[3] & ~pw[4], pw[4] & ~pw[3], pw[3] & pw[4], pw[5]};
+    const u64 cs[6] = {cp, cw[2], cw[3] & ~cw[4], cw[4] & ~cw[3], cw[3] & cw[4], cw[5]};
+    u64 h0 = kp.x, h1 = kp.y;
+#pragma unroll
+    for (int t = 0; t < 6; t++) {
+        for (u64 s = (ps[t] & pw[0]) ^ (cs[t] & cw[0]); s; s &= s - 1) {
+            const ulonglong2 e = z[t * 64 + zb_lsb(s)];
+            h0 ^= e.x;
+            h1 ^= e.y;
+        }
+        for (u64 s = (ps[t] & ~pw[0]) ^ (cs[t] & ~cw[0]); s; s &= s - 1) {
+            const ulonglong2 e = z[(6 + t) * 64 + zb_lsb(s)];
+            h0 ^= e.x;
+            h1 ^= e.y;
+        }
+    }
+    const u64 ds = pw[1] ^ cw[1];
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+        if ((ds >> c) & 1) {
+            h0 ^= z[Z_CASTLE + c].x;
+            h1 ^= z[Z_CASTLE + c].y;
+        }
+    const int pe = (int)((pw[1] >> 4) & 15), ce = (int)((cw[1] >> 4) & 15);
+    if (pe) {
+        h0 ^= z[Z_EP + ((pe - 1) & 7)].x;
+        h1 ^= z[Z_EP + ((pe - 1) & 7)].y;
+    }
+    if (ce) {
+        h0 ^= z[Z_EP + ((ce - 1) & 7)].x;
+        h1 ^= z[Z_EP + ((ce - 1) & 7)].y;
+    }
+    if (ds >> 63) {
+        h0 ^= z[Z_SIDE].x;
+        h1 ^= z[Z_SIDE].y;
+    }
+    if (!(h0 | h1)) h0 = 1;
+    return make_ulonglong2(h0, h1);
+}
+
 __host__ __device__ __forceinline__ u64 tt_mix(u64 k0, u64 k1) { return k0 ^ ((k1 << 29) | (k1 >> 35)); }
 
 // entry words for key (k0, k1) and count v

@@ -171,3 +171,44 @@ def test_entry_rejects_synthetic_low_word_collision_of_real_positions(pg):
 def test_tt_mode_values(pg):
     assert pg._tt_mode(True) == pg.TT_ON and pg._tt_mode(False) == pg.TT_OFF
     assert pg._tt_mode("dedup") == pg.TT_DEDUP_ONLY and pg._tt_mode(2) == 2
+
+
+def test_incremental_key_equals_full_key_for_every_child(pg, oracle):
+    """The probe kernel keys a node below the root from its parent's key
+    (pg_zobrist_key_from, the reference's incremental update in makeMove):
+    over every child of 300 walk positions (captures, castling, en passant,
+    promotions) and their grandchildren keyed from the updated key, the
+    update equals the full key."""
+    walk = golden_npz("walk.npz")["boards"]
+    kinds = 0
+    for w in walk[::4][:300]:
+        parent = pg.HexaBitBoardPosition(*(int(x) for x in w))
+        kp = pg.zobrist_key(parent)
+        for c in oracle.generate_boards(oracle_board(w)):
+            child = pg.HexaBitBoardPosition(*c)
+            kc = pg.zobrist_key_from(parent, kp, child)
+            assert kc == pg.zobrist_key(child) == _key_of_words(c)
+            kinds |= 1 << bin((int(w[1]) ^ c[1]) & 0x0F).count("1")  # castling rights cleared
+            for g in oracle.generate_boards(oracle_board(c))[:3]:
+                grand = pg.HexaBitBoardPosition(*g)
+                assert pg.zobrist_key_from(child, kc, grand) == pg.zobrist_key(grand)
+    assert kinds & 0b110, "no child cleared a castling right"
+
+
+def test_incremental_key_holds_for_any_two_boards_and_the_remapped_zero(pg):
+    """The update is exact for any pair of boards (XOR over the features that
+    differ), and a source key of (1, 0) -- which may stand for the raw key 0
+    -- falls back to the full key."""
+    walk = golden_npz("walk.npz")["boards"]
+    rng = random.Random(17)
+    for _ in range(300):
+        a, b = (walk[rng.randrange(len(walk))] for _ in range(2))
+        pa = pg.HexaBitBoardPosition(*(int(x) for x in a))
+        pb = pg.HexaBitBoardPosition(*(int(x) for x in b))
+        assert pg.zobrist_key_from(pa, pg.zobrist_key(pa), pb) == pg.zobrist_key(pb)
+        assert pg.zobrist_key_from(pa, (1, 0), pb) == pg.zobrist_key(pb)
+
+
+def oracle_board(words):
+    import oracle as O
+    return O.Board(*(int(x) for x in words))
