@@ -212,3 +212,20 @@ def test_incremental_key_holds_for_any_two_boards_and_the_remapped_zero(pg):
 def oracle_board(words):
     import oracle as O
     return O.Board(*(int(x) for x in words))
+
+
+def test_key_helpers_refuse_null_arguments(pg):
+    """The host-side key and entry helpers return PG_ERR_INVALID_ARGUMENT
+    for a null pointer, with a message, instead of reading through it."""
+    import ctypes
+    PG_ERR_INVALID_ARGUMENT = 2  # include/perft_gb300.h
+    lib = pg.load_library()
+    b = pg.board_from_fen(golden_json("fens.json")[0]["fen"])
+    k = (ctypes.c_uint64 * 2)()
+    assert lib.pg_zobrist_key(None, k) == PG_ERR_INVALID_ARGUMENT
+    assert lib.pg_zobrist_key_from(ctypes.byref(b), None, ctypes.byref(b), k) == PG_ERR_INVALID_ARGUMENT
+    assert lib.pg_zobrist_key_from(ctypes.byref(b), k, ctypes.byref(b), None) == PG_ERR_INVALID_ARGUMENT
+    assert b"null" in lib.pg_last_error()
+    e = (ctypes.c_uint64 * 4)()
+    assert lib.pg_tt_entry_pack(None, 5, e) == PG_ERR_INVALID_ARGUMENT
+    assert lib.pg_tt_entry_match(e, k, None, None) == PG_ERR_INVALID_ARGUMENT
