@@ -5,7 +5,9 @@
 // perft_bb.h:790-852; upsweep and stores perft_bb.h:854-961) re-planned for
 // the chunked breadth-first driver:
 //   * keys: 128-bit Zobrist keys (pg_zobrist.cuh: two seeded 64-bit words
-//     per feature, the shape of the reference's HashKey128b);
+//     per feature, the shape of the reference's HashKey128b), computed in
+//     full at the root level and below it updated from the parent's key by
+//     the features the move changed (the reference updates them in makeMove);
 //   * one table per remaining depth 2..9 of 32-byte entries that carry the
 //     count XORed into all 128 key bits (pg_zobrist.cuh), written as two
 //     16-byte stores; a foreign or torn entry is a miss, never a wrong count
