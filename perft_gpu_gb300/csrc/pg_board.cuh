@@ -262,7 +262,12 @@ __device__ __forceinline__ u64 ks_rook(u64 g, u64 empty)
 }
 
 // the four lines through a square (used to split pinned pieces by pin line)
-__device__ __forceinline__ u64 file_of(int sq) { return FILE_A << (sq & 7); }
+// both 32-bit halves of a file are the same: one 32-bit shift
+__device__ __forceinline__ u64 file_of(int sq)
+{
+    const u32 h = 0x01010101u << (sq & 7);
+    return ((u64)h << 32) | h;
+}
 __device__ __forceinline__ u64 rank_of(int sq) { return RANK_1 << (sq & 56); }
 __device__ __forceinline__ u64 diag_of(int sq)
 {
