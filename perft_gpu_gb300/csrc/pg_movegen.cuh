@@ -781,12 +781,21 @@ enum : u32 { PC_PAWN = 0, PC_KNIGHT = 1, PC_BISHOP = 2, PC_ROOK = 3, PC_QUEEN = 
 // with a double push: an enemy pawn stands beside the pushed pawn, so the
 // child's en-passant file is set (exact flagging, decided by the parent)
 constexpr u32 PC_EP_FLAG = 8;
-// a pawn move for the leaf: promotions N, B, Q, R (the reference's flags)
-// with the promoted piece as the landing piece
-template <class E> __device__ __forceinline__ void emit_pawn_leaf(E& emit, int from, u64 dst, int fl)
+// calls f(square) for every square of m in ascending order (the order of a
+// 64-bit lowest-bit loop), as two loops over the 32-bit halves: 32-bit
+// find-first-set and clear-lowest instead of their 64-bit forms, 1.2-1.4%
+// less leaf time (the leaf emits one queue entry per child)
+template <class F> __device__ __forceinline__ void each_square(u64 m, F&& f)
 {
-    const int to = lsb(dst);
-    if (dst & BACK_RANKS) {
+    for (u32 x = (u32)m; x; x &= x - 1) f(__ffs(x) - 1);
+    for (u32 x = (u32)(m >> 32); x; x &= x - 1) f(__ffs(x) + 31);
+}
+// a pawn move for the leaf, by target square: on rank 1 or 8 the promotions
+// N, B, Q, R (the reference's flags) with the promoted piece as the landing
+// piece
+template <class E> __device__ __forceinline__ void emit_pawn_sq(E& emit, int from, int to, int fl)
+{
+    if ((u32)(to - 8) >= 48u) {
         emit(cmove(from, to, fl | MF_PROMO_N), PC_KNIGHT);
         emit(cmove(from, to, fl | MF_PROMO_B), PC_BISHOP);
         emit(cmove(from, to, fl | MF_PROMO_Q), PC_QUEEN);
@@ -800,13 +809,11 @@ template <int S, class E> __device__ __forceinline__ void gen_from_facts(const P
 {
     const u64 tgt = f.tgt;
     const int ksq = f.ksq;
-    for (u64 m = __ldg(&g_king[ksq]) & ~(f.threat | f.mine); m; m &= m - 1)
-        emit(cmove(ksq, lsb(m), 0), PC_KING);
+    each_square(__ldg(&g_king[ksq]) & ~(f.threat | f.mine), [&](int to) { emit(cmove(ksq, to, 0), PC_KING); });
     const u64 pin_chk = f.pinned & f.chk_all;
     for (u64 s = b.n & f.mine & ~f.pinned; s; s &= s - 1) {
         const int sq = lsb(s);
-        for (u64 m = __ldg(&g_knight[sq]) & tgt; m; m &= m - 1)
-            emit(cmove(sq, lsb(m), 0), PC_KNIGHT);
+        each_square(__ldg(&g_knight[sq]) & tgt, [&](int to) { emit(cmove(sq, to, 0), PC_KNIGHT); });
     }
     // a pinned slider keeps the moves along its pin line (none if the line is
     // not its kind); in check pinned pieces do not move
@@ -816,7 +823,7 @@ template <int S, class E> __device__ __forceinline__ void gen_from_facts(const P
         u64 m = SlFancy::bishop(sq, f.occ) & tgt;
         if (f.pinned & bit) m &= (f.pd & bit) ? diag_of(ksq) : (f.pa & bit) ? anti_of(ksq) : 0ull;
         const u32 pc = (b.rq & bit) ? PC_QUEEN : PC_BISHOP;
-        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), 0), pc);
+        each_square(m, [&](int to) { emit(cmove(sq, to, 0), pc); });
     }
     for (u64 s = b.rq & f.mine & ~pin_chk; s; s &= s - 1) {
         const int sq = lsb(s);
@@ -824,7 +831,7 @@ template <int S, class E> __device__ __forceinline__ void gen_from_facts(const P
         u64 m = SlFancy::rook(sq, f.occ) & tgt;
         if (f.pinned & bit) m &= (f.pf & bit) ? file_of(ksq) : (f.pr & bit) ? rank_of(ksq) : 0ull;
         const u32 pc = (b.bq & bit) ? PC_QUEEN : PC_ROOK;
-        for (; m; m &= m - 1) emit(cmove(sq, lsb(m), 0), pc);
+        each_square(m, [&](int to) { emit(cmove(sq, to, 0), pc); });
     }
     // pawns, set-wise as in the count; from = to - step
     constexpr int PUSH = S ? -8 : 8, CW = S ? -9 : 7, CE = S ? -7 : 9;
@@ -832,17 +839,17 @@ template <int S, class E> __device__ __forceinline__ void gen_from_facts(const P
     const u64 fp = myp & ~f.pinned;
     const u64 pin_ok = ~f.chk_all;
     const u64 d1 = push1<S>(fp | (myp & f.pf & pin_ok)) & f.empty;
-    for (u64 m = d1 & tgt; m; m &= m - 1) emit_pawn_leaf(emit, lsb(m) - PUSH, lowbit(m), 0);
+    each_square(d1 & tgt, [&](int to) { emit_pawn_sq(emit, to - PUSH, to, 0); });
     const u64 their_pawns = f.pawns & f.theirs;
     for (u64 m = push1<S>(d1 & double_rank<S>() & ~f.safe) & f.empty & tgt; m; m &= m - 1) {
         const u64 t = lowbit(m);
         emit(cmove(lsb(m) - 2 * PUSH, lsb(m), MF_DOUBLE),
              PC_PAWN | (((east1(t) | west1(t)) & their_pawns) ? PC_EP_FLAG : 0u));
     }
-    for (u64 m = cap_w<S>(fp | (myp & (S ? f.pd : f.pa) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
-        emit_pawn_leaf(emit, lsb(m) - CW, lowbit(m), 0);
-    for (u64 m = cap_e<S>(fp | (myp & (S ? f.pa : f.pd) & pin_ok)) & f.theirs & tgt; m; m &= m - 1)
-        emit_pawn_leaf(emit, lsb(m) - CE, lowbit(m), 0);
+    each_square(cap_w<S>(fp | (myp & (S ? f.pd : f.pa) & pin_ok)) & f.theirs & tgt,
+                [&](int to) { emit_pawn_sq(emit, to - CW, to, 0); });
+    each_square(cap_e<S>(fp | (myp & (S ? f.pa : f.pd) & pin_ok)) & f.theirs & tgt,
+                [&](int to) { emit_pawn_sq(emit, to - CE, to, 0); });
     if (!f.checkers) {
         if (can_castle_k<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 62 : 6, MF_KCASTLE), PC_KING);
         if (can_castle_q<S>(b, f.occ, f.threat)) emit(cmove(S ? 60 : 4, S ? 58 : 2, MF_QCASTLE), PC_KING);
