@@ -74,8 +74,8 @@ __device__ __forceinline__ void set_side(Pos& b, int v) { b.p = (b.p & ~(1ull <<
 __device__ __forceinline__ void set_hm(Pos& b, int v) { b.p = (b.p & ~(0x7Full << 56)) | ((u64)(v & 0x7F) << 56); }
 
 // ---- left shifts on the FMA pipe ----
-// The move count is bound by integer-ALU issue (ALU pipe ~91% busy, FMA pipe
-// ~10%).  The propagator chains' 64-bit left shifts are written as 32-bit
+// The move count is bound by integer-ALU issue (ALU pipe ~88-91% busy, FMA
+// pipe ~10-14%).  The propagator chains' 64-bit left shifts are written as 32-bit
 // multiplies by 2^K read from __constant__ memory, which the compiler cannot
 // turn back into shifts: the low word one multiply, the high word one
 // multiply-add of the bits carried over from the low word (one ALU shift).

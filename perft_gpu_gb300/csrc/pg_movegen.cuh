@@ -46,8 +46,8 @@ static __device__ u64 g_knight_t[65];
 static __device__ u64 g_king[64];
 static __device__ u64 g_diag[64];
 static __device__ u64 g_pawn_checks[2][64];
-// The count is bound by integer-ALU issue (the ALU pipe ~91% busy, the FMA
-// pipe ~10%).  Its popcount sums are written as multiply-adds by a 1 the
+// The count is bound by integer-ALU issue (the ALU pipe ~88-91% busy, the
+// FMA pipe ~10-14%).  Its popcount sums are written as multiply-adds by a 1 the
 // compiler cannot fold (a __constant__ word), so they issue on the FMA pipe
 // instead of as ALU adds (measured 0.6% less leaf time on the batched
 // workload).
