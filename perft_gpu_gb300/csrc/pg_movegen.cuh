@@ -1062,14 +1062,6 @@ __device__ __forceinline__ void make_move(Pos& b, u16 mv)
     }
 }
 
-// makeMove for a child whose moves are only counted: it writes what the count
-// for the side to move next reads (the pieces, that side's castling rights
-// and the exact en-passant file, as make_move) and leaves the mover's own
-// castling rights and the side bit as they were.  `piece` is the moving piece
-// that lands on the target square (PC_*; the promoted piece for a
-// promotion), so nothing is looked up on the board or decoded from the flags,
-// plus PC_EP_FLAG on a double push that gives the opponent an en-passant
-// capture.
 // the bit of square s (0..63) from two 32-bit shifts: PTX clamps a shift
 // amount of 32 or more to 32, which clears the word, so the half that does
 // not hold the square is 0 with no select (0.2-0.3% less leaf time than the
@@ -1081,6 +1073,15 @@ __device__ __forceinline__ u64 bit64(u32 s)
     asm("shl.b32 %0, %1, %2;" : "=r"(hi) : "r"(1u), "r"(s - 32u));
     return ((u64)hi << 32) | lo;
 }
+
+// makeMove for a child whose moves are only counted: it writes what the count
+// for the side to move next reads (the pieces, that side's castling rights
+// and the exact en-passant file, as make_move) and leaves the mover's own
+// castling rights and the side bit as they were.  `piece` is the moving piece
+// that lands on the target square (PC_*; the promoted piece for a
+// promotion), so nothing is looked up on the board or decoded from the flags,
+// plus PC_EP_FLAG on a double push that gives the opponent an en-passant
+// capture.
 template <int S>
 __device__ __forceinline__ void make_child(Pos& b, u16 mv, u32 piece)
 {
